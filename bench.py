@@ -1,0 +1,435 @@
+"""Benchmark of the StatER statistics hot path on GB300.
+
+Workload (default): 1920x1080 image, 256 samples per pixel, five monotone
+transforms (identity, log1p, sqrt, cbrt, asinh) of RGB radiance, 7 feature
+channels (albedo RGB, normal xyz, depth), moments M1-M3, 21x21 window (R=10),
+Welch alpha = 0.01, range kernels on albedo (sigma 0.02), normal (0.1), depth
+(0.1). One step = accumulate all samples into fresh moment buffers, the
+variance-denoise pass, and the Welch-discriminated film filter, in the FP32
+form. Samples are seeded synthetic planes (25.5 GB, larger than L2), resident in
+HBM for `value`; `e2e` streams them from pinned host memory every step through
+the same public API (chunked host-to-device copies overlapping the
+accumulation) and reads the denoised image back.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl stater|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mpix/s denoised (1080p, 5 transforms)"
+UNIT = "Mpix/s"
+WORKLOAD = dict(width=1920, height=1080, spp=256, transforms=["identity", "log1p", "sqrt", "cbrt", "asinh"],
+                features=7, max_moment=3, radius=10, filter_sd=10.0, alpha=0.01, var_z=2.80703,
+                gbuffers=[(0, 3, 0.02), (3, 3, 0.1), (6, 1, 0.1)])
+LAUNCHES_PER_STEP = 5  # accumulate 1, denoise_vars 2, denoise_film 2
+
+
+def _config(extra=None):
+    w = WORKLOAD
+    c = {"workload": f"multi-transform denoise {w['width']}x{w['height']} {w['spp']}spp K=5 G=7 M1-M3 "
+                     f"{2 * w['radius'] + 1}x{2 * w['radius'] + 1} alpha={w['alpha']}",
+         "width": w["width"], "height": w["height"], "spp": w["spp"], "transforms": w["transforms"],
+         "features": w["features"], "window": 2 * w["radius"] + 1, "alpha": w["alpha"],
+         "l2": "inputs larger than L2 (25.5 GB sample planes per image)", "parallelism": "replicas"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU pipeline (the reference's CPU path for stage 1, the oracle for 2-3)
+# ---------------------------------------------------------------------------
+def cpu_pipeline_mpix(samples_host, threads):
+    """Times the CPU restatement on a strip: FP32 StatTile port (the reference's
+    CPU accumulation) + FP64 denoise restatement. Returns (Mpix/s, seconds)."""
+    import numpy as np
+
+    import oracle
+    w = WORKLOAD
+    S, nch, H, W = samples_host.shape
+    K = len(w["transforms"])
+    n = np.zeros((H, W), np.int32)
+    st32 = np.zeros((K, 7, 3, H, W), np.float32)
+    g32 = np.zeros((w["features"], H, W), np.float32)
+    ds = float(np.float32(-0.5 / (w["filter_sd"] ** 2)))
+    t0 = time.perf_counter()
+    oracle.accumulate(samples_host, w["transforms"], w["max_moment"], n, st32, g32, precision="f32",
+                      nthreads=threads)
+    st = st32.astype(np.float64)
+    gm = g32.astype(np.float64)
+    v = oracle.denoise_vars(n, st, gm, w["max_moment"], w["radius"], ds, float(np.float32(w["var_z"])),
+                            w["gbuffers"], nthreads=threads)
+    oracle.denoise_film(n, st, v["varD"], v["varCD"], v["jb"], gm, st[0, 0], w["radius"], ds,
+                        float(np.float32(w["alpha"])), w["gbuffers"], nthreads=threads)
+    dt = time.perf_counter() - t0
+    return H * W / dt / 1e6, dt
+
+
+def strip_samples(rows, seed=0):
+    """Samples of a 1920 x rows strip of the workload (host float32)."""
+    import numpy as np
+    import torch
+
+    import stater_gb300 as S
+    w = WORKLOAD
+    if torch.cuda.is_available():
+        return S.generate_samples(w["width"], rows, w["spp"], n_features=w["features"], seed=seed).cpu().numpy()
+    sys.path.insert(0, str(ROOT / "tests"))
+    from helpers import synth_samples
+    return synth_samples(w["width"], rows, w["spp"], G=w["features"], seed=seed, region=8).astype(np.float32)
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    rows = args.cpu_rows
+    smp = strip_samples(rows, seed=1)
+    for _ in range(args.warmup):
+        cpu_pipeline_mpix(smp[:, :, : max(2, rows // 4)], threads)
+    vals = []
+    for _ in range(args.steps):
+        v, _ = cpu_pipeline_mpix(smp, threads)
+        vals.append(v)
+    value = statistics.median(vals)
+    sample = f"1920x{rows} strip of the workload per step ({args.spp_note})"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1920 * rows / value / 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
+            "config": _config(),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+def _specs(S):
+    return [S.GBufferSpec(a, c, sg) for a, c, sg in WORKLOAD["gbuffers"]]
+
+
+def _denoise(S, b, stream=None):
+    w = WORKLOAD
+    b.denoise_vars(radius=w["radius"], filter_sd=w["filter_sd"], var_z=w["var_z"], gbuffers=_specs(S), stream=stream)
+    b.denoise_film(radius=w["radius"], filter_sd=w["filter_sd"], alpha=w["alpha"], gbuffers=_specs(S), stream=stream)
+
+
+def _reset(b):
+    b.n.zero_()
+    b.stats.zero_()
+    b.gmean.zero_()
+
+
+def run_gpu(args, rank, world, dist):
+    import numpy as np
+    import torch
+
+    import stater_gb300 as S
+    from __graft_entry__ import build
+    if rank == 0 or not (ROOT / "stater_gb300" / "libstater.so").exists():
+        build()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    S.setup()
+    w = WORKLOAD
+    W, H, SPP, G, K = w["width"], w["height"], w["spp"], w["features"], len(w["transforms"])
+    HW = W * H
+    stream = torch.cuda.current_stream()
+
+    samples = S.generate_samples(W, H, SPP, n_features=G, seed=1234 + rank)
+    b = S.StatBuffers(W, H, w["transforms"], G, w["max_moment"], S.F32)
+
+    def step():
+        _reset(b)
+        b.accumulate(samples, mode=S.ACC_FAST)
+        _denoise(S, b)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # per-stage kernel timings (CUDA events on the launching stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    stage_ms = {"accumulate": [], "denoise_vars": [], "denoise_film": []}
+    for _ in range(3):
+        _reset(b)
+        ev[0].record(stream)
+        b.accumulate(samples, mode=S.ACC_FAST)
+        ev[1].record(stream)
+        b.denoise_vars(radius=w["radius"], filter_sd=w["filter_sd"], var_z=w["var_z"], gbuffers=_specs(S))
+        ev[2].record(stream)
+        b.denoise_film(radius=w["radius"], filter_sd=w["filter_sd"], alpha=w["alpha"], gbuffers=_specs(S))
+        ev[3].record(stream)
+        torch.cuda.synchronize()
+        stage_ms["accumulate"].append(ev[0].elapsed_time(ev[1]))
+        stage_ms["denoise_vars"].append(ev[1].elapsed_time(ev[2]))
+        stage_ms["denoise_film"].append(ev[2].elapsed_time(ev[3]))
+
+    # timed region
+    steps = args.steps
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        evs[0].record(stream)
+        for i in range(steps):
+            step()
+            evs[i + 1].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    per_step = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
+    total_ms = evs[0].elapsed_time(evs[steps])
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * HW * steps / (total_ms / 1e3) / 1e6
+    filmD_check = float(b.filmD.double().mean().item())
+
+    # roofline of the accumulation kernel (HBM-bound): algorithmic bytes per launch
+    acc_bytes = HW * (SPP * (5 + G) * 4 + 2 * (K * 3 * w["max_moment"] * 4 + G * 4 + 4))
+    acc_ms = statistics.median(stage_ms["accumulate"])
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    roofline = {"kernel": "acc_kernel (stage-1 accumulation)", "bound": "hbm",
+                "achieved": acc_bytes / (acc_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "frac": acc_bytes / (acc_ms / 1e3) / 1e9 / hbm_peak, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback"}
+
+    del samples
+    torch.cuda.empty_cache()
+
+    extra = {}
+    # plain FP64 form (one image per launch), same workload
+    if not args.no_plain:
+        pb = S.StatBuffers(W, H, w["transforms"], G, w["max_moment"], S.F64)
+        chunk = 32
+        samples_c = torch.empty(chunk, 5 + G, H, W, dtype=torch.float32, device="cuda")
+        first = torch.zeros(H, W, dtype=torch.int32, device="cuda")
+
+        def plain_step(timed_events=None):
+            _reset(pb)
+            for c0 in range(0, SPP, chunk):
+                first.fill_(c0)
+                S.generate_samples(W, H, chunk, n_features=G, seed=1234 + rank, first_index=first, out=samples_c)
+                if timed_events is not None:
+                    timed_events[0].record(stream)
+                pb.accumulate(samples_c, mode=S.ACC_EXACT)
+                if timed_events is not None:
+                    timed_events[1].record(stream)
+                    torch.cuda.synchronize()
+                    timed_events[2] += timed_events[0].elapsed_time(timed_events[1])
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _denoise(S, pb)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1)
+
+        plain_step()
+        accs, dens = [], []
+        for _ in range(args.plain_steps):
+            te = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True), 0.0]
+            dms = plain_step(te)
+            accs.append(te[2])
+            dens.append(dms)
+        plain_ms = statistics.median([a + d for a, d in zip(accs, dens)])
+        extra["plain_f64"] = {"value": HW / (plain_ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": plain_ms,
+                              "accumulate_ms": statistics.median(accs), "denoise_ms": statistics.median(dens),
+                              "note": "FP64, one image per launch, sample generation excluded"}
+        extra["speedup_vs_plain_f64"] = value / world / extra["plain_f64"]["value"]
+        del pb, samples_c
+        torch.cuda.empty_cache()
+
+    # end to end through the public API with pinned host samples
+    e2e = None
+    if not args.no_e2e:
+        chunk = 16
+        host = torch.empty(SPP, 5 + G, H, W, dtype=torch.float32, pin_memory=True)
+        first = torch.zeros(H, W, dtype=torch.int32, device="cuda")
+        tmp = torch.empty(chunk, 5 + G, H, W, dtype=torch.float32, device="cuda")
+        for c0 in range(0, SPP, chunk):
+            first.fill_(c0)
+            S.generate_samples(W, H, chunk, n_features=G, seed=1234 + rank, first_index=first, out=tmp)
+            host[c0:c0 + chunk].copy_(tmp)
+        del tmp
+        out_host = torch.empty(3, H, W, dtype=torch.float32, pin_memory=True)
+        stage = [torch.empty(chunk, 5 + G, H, W, dtype=torch.float32, device="cuda") for _ in range(2)]
+        copy_stream = torch.cuda.Stream()
+        free = [torch.cuda.Event(), torch.cuda.Event()]
+        ready = [torch.cuda.Event(), torch.cuda.Event()]
+        for e in free:
+            e.record(stream)
+
+        def e2e_step():
+            _reset(b)
+            for ci, c0 in enumerate(range(0, SPP, chunk)):
+                s = ci % 2
+                copy_stream.wait_event(free[s])
+                with torch.cuda.stream(copy_stream):
+                    stage[s].copy_(host[c0:c0 + chunk], non_blocking=True)
+                ready[s].record(copy_stream)
+                stream.wait_event(ready[s])
+                b.accumulate(stage[s], mode=S.ACC_FAST)
+                free[s].record(stream)
+            _denoise(S, b)
+            out_host.copy_(b.filmD, non_blocking=True)
+
+        for _ in range(args.warmup):
+            e2e_step()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
+        e2e_val = HW / (e2e_ms / 1e3) / 1e6
+        if world > 1:
+            t = torch.tensor([e2e_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_val = world * HW / (float(t.item()) / 1e3) / 1e6
+        e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": SPP * (5 + G) * HW * 4,
+               "d2h_bytes_per_step": 3 * HW * 4, "ms_per_step": e2e_ms,
+               "path": "pinned host samples -> 16-spp chunks (copy stream) -> accumulate -> denoise -> filmD to host"}
+        del host, stage
+        torch.cuda.empty_cache()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        smp = strip_samples(args.cpu_rows, seed=1)
+        v, secs = cpu_pipeline_mpix(smp, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"1920x{args.cpu_rows} strip of the workload, {secs:.1f} s (FP32 StatTile port + FP64 "
+                         f"denoise restatement)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox planes)",
+                "config": _config(), "latency_ms": {"p50": float(np.percentile(per_step, 50)),
+                                                     "p99": float(np.percentile(per_step, 99))},
+                "stage_ms": {k: statistics.median(v) for k, v in stage_ms.items()},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": LAUNCHES_PER_STEP * steps, "clocks": clk.summary(), "checksum_filmD_mean": filmD_check}
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="stater", choices=["stater", "reference"])
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-rows", type=int, default=32)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    args.spp_note = f"{WORKLOAD['spp']} spp"
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "stater" else "gloo"
+        dist.init_process_group(backend)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank)
+        else:
+            run_gpu(args, rank, world, dist)
+    finally:
+        if dist is not None and dist.is_initialized():
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,288 @@
+/*
+ * stater: GB300-native (sm_103a) statistics hot path of StatER.
+ *
+ * C ABI of libstater.so. Plain pointers and sizes only; every call returns a
+ * stater_status and never aborts. All image buffers are planar: a "plane" holds
+ * W*H elements with pixel p = y*W + x, and an RGB statistics buffer ("float3
+ * buffer" in the reference) is three consecutive planes (R, G, B). Element type
+ * of the statistics buffers is chosen per call by `precision`: STATER_F64 is the
+ * plain FP64 form, STATER_F32 the FP32 form. Sample counts are int32, as the
+ * reference's t?-b?-film-n buffer (estimator.h:477).
+ *
+ * Reference boundary replaced (paths inside the StatER tree):
+ *   cv::cuda::stat_denoiser::setup()               src/statistics/estimator.h:383
+ *   cv::cuda::stat_denoiser::denoiseVars<float3>   src/statistics/estimator.cpp:374-414
+ *   cv::cuda::stat_denoiser::denoiseFilm           src/statistics/estimator.cpp:421-457
+ *   cv::cuda::stat_denoiser::calcTargetSPP<float3> src/statistics/estimator.cpp:502-511
+ *   cv::cuda::stat_denoiser::synchronize           src/statistics/estimator.cpp:516
+ *   cv::cuda::stat_denoiser::printMacroConfiguration src/statistics/estimator.cpp:520
+ * and, moved from the CPU onto the GPU:
+ *   StatTile::AddTransformSample* / AddSample*     src/statistics/estimator.h:226-324
+ *   Estimator::MergeTransformTile / MergeTile      src/statistics/estimator.cpp:267-324
+ *   Estimator::CalcMeanVars (calcMatMeanVar)       src/statistics/estimator.cpp:462-496
+ */
+#ifndef STATER_H
+#define STATER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STATER_ABI_VERSION 1
+#define STATER_MAX_TRANSFORMS 8 /* buffers b0..b7 per statistics type */
+#define STATER_MAX_GBUFFERS 8
+#define STATER_MAX_FEATURES 16
+#define STATER_MAX_RADIUS 20   /* the reference default filterradius */
+
+typedef struct CUstream_st *stater_stream; /* a cudaStream_t; NULL = legacy default stream */
+
+typedef enum {
+    STATER_OK = 0,
+    STATER_ERR_INVALID = 1,     /* bad argument (message in stater_last_error) */
+    STATER_ERR_CUDA = 2,        /* a CUDA call failed */
+    STATER_ERR_NOMEM = 3,       /* device scratch could not be allocated */
+    STATER_ERR_UNSUPPORTED = 4, /* configuration outside what this build handles */
+    STATER_ERR_TIMEOUT = 5      /* a bounded device wait gave up */
+} stater_status;
+
+typedef enum { STATER_F32 = 0, STATER_F64 = 1 } stater_precision;
+
+/* Monotone transforms applied to radiance samples. Transform 0 of every job must
+ * be STATER_TK_IDENTITY: it is the untransformed "t0 / film" set of the reference. */
+typedef enum {
+    STATER_TK_IDENTITY = 0,
+    STATER_TK_LOG1P = 1,
+    STATER_TK_SQRT = 2,
+    STATER_TK_CBRT = 3,
+    STATER_TK_ASINH = 4,
+    STATER_TK_BOXCOX = 5 /* (x^lambda - 1) / lambda, identity at lambda == 1 (estimator.h:43-76) */
+} stater_transform_kind;
+
+/* Moment planes of one transform, in this order, 3 planes each. */
+typedef enum {
+    STATER_Q_MEAN = 0, STATER_Q_M2 = 1, STATER_Q_M3 = 2, STATER_Q_M4 = 3,
+    STATER_Q_C2X = 4, STATER_Q_C2Y = 5, STATER_Q_M1 = 6, STATER_NQ = 7
+} stater_moment;
+
+/* How the Welch decisions of several transforms combine in denoiseFilm; the
+ * values are those of the reference's FILM_MULTI_TRANSFORM_MODE switch
+ * (src/statistics/statpbrt.h:27-29, estimator.cpp:446-448). */
+typedef enum {
+    STATER_MT_ALL = 2, /* neighbour kept only if every transform accepts it */
+    STATER_MT_JB = 3   /* only the transform with the lowest Jarque-Bera score at the centre */
+} stater_mt_mode;
+
+typedef enum {
+    STATER_ACC_EXACT = 0, /* the reference's operation order: x/n division, libm-accurate transforms */
+    STATER_ACC_FAST = 1   /* FP32 only: reciprocal of n shared per sample, fast transforms */
+} stater_acc_mode;
+
+typedef struct {
+    int32_t kind;   /* stater_transform_kind */
+    float lambda;   /* Box-Cox lambda (float, as the reference's lambdas list) */
+} stater_transform;
+
+/* G-buffers used by a range kernel (estimator.cpp:10-18, 69-81): each entry is
+ * `channels` (1 or 3) consecutive planes with the element type of the call. */
+typedef struct {
+    int32_t count;
+    const void *planes[STATER_MAX_GBUFFERS];
+    int32_t channels[STATER_MAX_GBUFFERS];
+    float dr_factor[STATER_MAX_GBUFFERS]; /* -0.5 / sigma_r^2 */
+} stater_gbuffers;
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* stat_denoiser::setup(): selects the current device, checks that it is an
+ * sm_103 part and prepares per-device state. Idempotent. */
+stater_status stater_setup(void);
+/* stat_denoiser::synchronize(stream). */
+stater_status stater_synchronize(stater_stream stream);
+/* stat_denoiser::printMacroConfiguration(): prints the runtime configuration
+ * that replaces the reference's compile-time macros. */
+void stater_print_macro_configuration(void);
+/* Message of the last failing call on this thread ("" if none). */
+const char *stater_last_error(void);
+int32_t stater_abi_version(void);
+/* Releases cached device scratch and tables of the current device. */
+stater_status stater_release_cache(void);
+
+/* ---- stage 1: moment accumulation ------------------------------------- */
+
+/* Per-sample statistics update of StatTile (estimator.h:226-324), for a whole
+ * image at once. Samples are float32 planes [S][5+G][W*H]: R, G, B, the
+ * in-pixel position u, v (inPxP, statpath.cpp:339) and G feature channels.
+ * For pixel p only the first count[p] sample planes are used (count == NULL:
+ * all S). Statistics persist in the caller's buffers, so later calls continue
+ * the same online update, as the reference's tiles do across iterations
+ * (statpath.cpp:133-150). n is incremented once per sample.
+ *   stats: precision-typed [K][7][3][W*H] (transform, moment, channel, pixel)
+ *   gmean: precision-typed [G][W*H] running mean of every feature channel
+ *          (AddSampleM1 of the G-buffer tiles, statpath.cpp:366-379); may be NULL if G == 0
+ * max_moment: 1..5 as the reference's "maxmoment" (statpath.cpp:36-60; 5 = M4 + c2X, c2Y, m1). */
+typedef struct {
+    int32_t width, height;
+    int32_t n_samples;          /* S */
+    int32_t n_features;         /* G */
+    const float *samples;
+    const int32_t *count;       /* nullable */
+    int32_t n_transforms;       /* K */
+    stater_transform transforms[STATER_MAX_TRANSFORMS];
+    int32_t max_moment;
+    stater_precision precision;
+    int32_t mode;               /* stater_acc_mode */
+    int32_t *n;
+    void *stats;
+    void *gmean;
+} stater_accumulate_args;
+stater_status stater_accumulate(const stater_accumulate_args *a, stater_stream stream);
+
+/* Seeded synthetic sample source (stands in for the renderer): writes sample
+ * planes [S][5+G][W*H] for sample indices first_index[p] + s (first_index may be
+ * NULL = 0), counter-based (Philox4x32-10) so that any sample of any pixel can be
+ * regenerated. Radiance = per-region lognormal mean x lognormal(0, sigma) with
+ * firefly_prob fireflies scaled by firefly_scale; u,v uniform; features piecewise
+ * constant per region plus small jitter, or, with lev_r2 > 0, uniform per sample
+ * with radiance linear in the features (target R^2 = lev_r2). */
+typedef struct {
+    int32_t width, height, n_samples, n_features;
+    uint64_t seed;
+    int32_t region;             /* side of the square regions sharing a mean (1 = per pixel) */
+    float mean_mu, mean_sigma;  /* per-region mean ~ LogNormal(mean_mu, mean_sigma) */
+    float noise_sigma;          /* per-sample factor ~ LogNormal(0, noise_sigma) */
+    float firefly_prob, firefly_scale;
+    float lev_r2;               /* 0 = off */
+    const int32_t *first_index; /* nullable */
+    float *samples;
+} stater_generate_args;
+stater_status stater_generate_samples(const stater_generate_args *a, stater_stream stream);
+
+/* Estimator::MergeTransformTile / MergeTile (estimator.cpp:267-324): copies CPU
+ * tile records into the image planes. records: raw StatTilePixel<Vec3> of the
+ * reference's float build (320 bytes: uint64 n at 0, t0 at 64, t1 at 192, seven
+ * float3 each), for every tile in order, pixels row-major in the tile. bounds:
+ * int32 [n_tiles][4] = x0, y0, x1, y1 (exclusive). Writes n and FP32 stats
+ * [n_sets][7][3][W*H], n_sets = 2 (transform tile) or 1 (plain tile). Device pointers. */
+stater_status stater_merge_tiles(int32_t width, int32_t height, int32_t n_tiles,
+                                 const int32_t *bounds, const void *records, int32_t n_sets,
+                                 int32_t *n, float *stats, stater_stream stream);
+
+/* Pairwise combine of two moment sets of the same geometry (Chan et al.;
+ * Pebay 2008): A <- A (+) B, for merging independently accumulated rounds or
+ * partial tiles. stats as in stater_accumulate. */
+stater_status stater_merge_moments(int32_t width, int32_t height, int32_t n_transforms,
+                                   int32_t max_moment, stater_precision precision, int32_t *nA,
+                                   void *statsA, const int32_t *nB, const void *statsB,
+                                   stater_stream stream);
+
+/* ---- stage 2: denoising ------------------------------------------------- */
+
+/* stat_denoiser::denoiseVars<float3> (estimator.cpp:374-414). For every
+ * transform b < n_buffers (pointer tables indexed by b, each an RGB buffer):
+ * per-pixel Jarque-Bera score jb (one plane per buffer, BUF_LIST estimator.h:467),
+ * Bonett lnS2 and se2, LEV-corrected m2C, and the variance filter outputs varD and
+ * varCD. m2C_in (nullable) replaces the c2X/c2Y correction of buffer 0 by an
+ * external LEV result (stater_lev_solve). */
+typedef struct {
+    int32_t n_buffers;
+    int32_t width, height;
+    int32_t filter_radius;
+    float ds_factor;            /* -0.5 / filtersd^2 (estimator.h:353) */
+    float var_z;                /* "varzvalue" (statpath.cpp:1070), default 2.80703 */
+    int32_t max_moment;
+    stater_precision precision;
+    const int32_t *n;
+    const void *m2[STATER_MAX_TRANSFORMS];
+    const void *m3[STATER_MAX_TRANSFORMS];
+    const void *m4[STATER_MAX_TRANSFORMS];   /* used when max_moment >= 4 */
+    const void *c2X[STATER_MAX_TRANSFORMS];  /* used when max_moment >= 5 */
+    const void *c2Y[STATER_MAX_TRANSFORMS];
+    const void *m2C_in;
+    stater_gbuffers gbuffers;
+    void *jb[STATER_MAX_TRANSFORMS];
+    void *lnS2[STATER_MAX_TRANSFORMS];
+    void *se2[STATER_MAX_TRANSFORMS];
+    void *m2C[STATER_MAX_TRANSFORMS];
+    void *varD[STATER_MAX_TRANSFORMS];
+    void *varCD[STATER_MAX_TRANSFORMS];
+} stater_denoise_vars_args;
+stater_status stater_denoise_vars(const stater_denoise_vars_args *a, stater_stream stream);
+
+/* stat_denoiser::denoiseFilm (estimator.cpp:421-457). Welch-discriminated
+ * neighbourhood filter of the film. Buffer 0 uses `film` as its mean, as the
+ * reference passes filmBuffer for the untransformed set; buffers b >= 1 use
+ * mean[b]. Writes the per-pixel Welch discriminator discr[b] (squared standard
+ * error of the mean) and filmD. accept_bits (nullable, debug): uint32
+ * [W*H][n_buffers][ceil((2R+1)^2/32)], bit (dy+R)(2R+1)+(dx+R) set when
+ * transform b accepts that neighbour. */
+typedef struct {
+    int32_t n_buffers;
+    int32_t width, height;
+    int32_t filter_radius;
+    float ds_factor;
+    float alpha;                /* two-sided level of the Welch test, e.g. 0.01 */
+    int32_t mt_mode;            /* stater_mt_mode */
+    int32_t use_levc;           /* 1: test with varCD, 0: with varD */
+    stater_precision precision;
+    const int32_t *n;
+    const void *film;
+    const void *mean[STATER_MAX_TRANSFORMS];  /* [0] unused */
+    const void *varD[STATER_MAX_TRANSFORMS];
+    const void *varCD[STATER_MAX_TRANSFORMS];
+    const void *jb[STATER_MAX_TRANSFORMS];    /* used by STATER_MT_JB */
+    stater_gbuffers gbuffers;
+    void *discr[STATER_MAX_TRANSFORMS];
+    void *filmD;
+    uint32_t *accept_bits;
+} stater_denoise_film_args;
+stater_status stater_denoise_film(const stater_denoise_film_args *a, stater_stream stream);
+
+/* Squared two-sided Student-t critical values over u = 1/df: table[m] =
+ * t_{1-alpha/2}(N/m)^2 (table[0] = z^2), m = 0..N, N = lut_intervals. The Welch
+ * test of stater_denoise_film interpolates this table linearly in u. Host memory. */
+int32_t stater_tcrit_lut_intervals(void);
+stater_status stater_tcrit2_table(double alpha, double *table);
+double stater_t_quantile(double p, double df);
+
+/* stat_denoiser::calcTargetSPP<float3> (estimator.cpp:502-511): extra samples
+ * for the next adaptive round. e_p = sum_c varD_c / n_p (divided by mean_c^2 +
+ * eps when mean != NULL); target_p = clamp(rint(spp * W*H * e_p / sum e), tmin,
+ * tmax), the sum by a fixed-order tree so that the result is deterministic.
+ * varD and mean are RGB buffers of the call's precision. */
+stater_status stater_calc_target_spp(int32_t width, int32_t height, int32_t spp,
+                                     stater_precision precision, const int32_t *n,
+                                     const void *varD, const void *mean, double eps,
+                                     int32_t tmin, int32_t tmax, int32_t *targetspp,
+                                     stater_stream stream);
+
+/* Estimator::CalcMeanVars / calcMatMeanVar (estimator.cpp:462-496):
+ * meanVar = m2 / ((n - 1) * n) in float arithmetic. RGB buffers. */
+stater_status stater_calc_mean_var(int32_t width, int32_t height, const int32_t *n,
+                                   const float *m2, float *mean_var, stater_stream stream);
+
+/* ---- stage 3: linear explained variance ------------------------------- */
+
+/* Per-pixel regression of the three radiance channels on the G feature channels
+ * plus an intercept. Accumulation keeps, per pixel, n, a pivot sample and the
+ * pivot-shifted sums and cross-products (stater_lev_state_size values, planes
+ * of W*H). STATER_F64 accumulates in FP64; STATER_F32 in FP32 with blocked
+ * Kahan-compensated sums (hi and lo planes, 2 * state size). The solve is FP64:
+ * ridge with lambda on the slopes, Cholesky. Outputs (precision-typed):
+ * beta [3][G+1][W*H] (intercept first), m2C [3][W*H] = residual sum of squares,
+ * r2 [3][W*H]. */
+int32_t stater_lev_state_size(int32_t n_features, stater_precision precision);
+stater_status stater_lev_accumulate(int32_t width, int32_t height, int32_t n_features,
+                                    int32_t n_samples, const float *samples,
+                                    const int32_t *count, stater_precision precision,
+                                    void *state, stater_stream stream);
+stater_status stater_lev_solve(int32_t width, int32_t height, int32_t n_features,
+                               stater_precision precision, const void *state, double lambda,
+                               void *beta, void *m2C, void *r2, stater_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,263 @@
+"""Python front end of libstater over device-resident torch tensors.
+
+`StatBuffers` holds the statistics buffers of one image the way the reference's
+Estimator does (estimator.h:459-519, estimator.cpp:83-245): per transform b and
+per BUF_LIST name one RGB buffer, plus the per-pixel sample count n. Here every
+buffer is a planar [3, H, W] slice of one contiguous tensor, so pointer tables
+for the C ABI are plain offsets.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import torch
+
+from . import _lib as L
+
+TRANSFORM_NAMES = {"identity": L.TK_IDENTITY, "log1p": L.TK_LOG1P, "sqrt": L.TK_SQRT,
+                   "cbrt": L.TK_CBRT, "asinh": L.TK_ASINH, "boxcox": L.TK_BOXCOX}
+
+# The five monotone transforms of the multi-transform configuration.
+BASELINE_TRANSFORMS = (("identity", 1.0), ("log1p", 1.0), ("sqrt", 1.0), ("cbrt", 1.0), ("asinh", 1.0))
+# The reference's default single Box-Cox build: t0 raw + t1 Box-Cox(0.25) (estimator.h:48-56).
+REFERENCE_TRANSFORMS = (("identity", 1.0), ("boxcox", 0.25))
+
+
+def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
+    if t is None:
+        return None
+    return t.data_ptr()
+
+
+def _stream_ptr(stream: Optional[torch.cuda.Stream]) -> Optional[int]:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return stream.cuda_stream or None
+
+
+def _dtype(precision: int) -> torch.dtype:
+    return torch.float64 if precision == L.F64 else torch.float32
+
+
+def transform_codes(transforms: Sequence) -> list[tuple[int, float]]:
+    out = []
+    for t in transforms:
+        if isinstance(t, str):
+            out.append((TRANSFORM_NAMES[t], 1.0))
+        else:
+            name, lam = t
+            out.append((TRANSFORM_NAMES[name] if isinstance(name, str) else int(name), float(lam)))
+    return out
+
+
+@dataclass
+class GBufferSpec:
+    """A G-buffer for a range kernel: `channels` feature channels starting at
+    `first` in the feature-mean planes, with range standard deviation `sigma`
+    (dr factor -0.5/sigma^2, estimator.cpp:10-18)."""
+    first: int
+    channels: int
+    sigma: float
+
+
+# albedo RGB, normal xyz, depth (feature channel order of the synthetic scenes)
+GBUFFERS_ALBEDO_NORMAL = (GBufferSpec(0, 3, 0.02), GBufferSpec(3, 3, 0.1))
+GBUFFERS_ALL7 = (GBufferSpec(0, 3, 0.02), GBufferSpec(3, 3, 0.1), GBufferSpec(6, 1, 0.1))
+
+
+class StatBuffers:
+    """Device buffers of one image: moments, feature means and denoiser outputs."""
+
+    def __init__(self, width: int, height: int, transforms=BASELINE_TRANSFORMS, n_features: int = 7,
+                 max_moment: int = 3, precision: int = L.F32, device="cuda"):
+        self.W, self.H = int(width), int(height)
+        self.HW = self.W * self.H
+        self.transforms = transform_codes(transforms)
+        self.K = len(self.transforms)
+        self.G = int(n_features)
+        self.max_moment = int(max_moment)
+        self.precision = int(precision)
+        dt = _dtype(precision)
+        dev = torch.device(device)
+        H, W, K = self.H, self.W, self.K
+        self.n = torch.zeros(H, W, dtype=torch.int32, device=dev)
+        self.stats = torch.zeros(K, L.NQ, 3, H, W, dtype=dt, device=dev)
+        self.gmean = torch.zeros(max(self.G, 1), H, W, dtype=dt, device=dev)
+        self.jb = torch.zeros(K, H, W, dtype=dt, device=dev)
+        self.lnS2 = torch.zeros(K, 3, H, W, dtype=dt, device=dev)
+        self.se2 = torch.zeros_like(self.lnS2)
+        self.m2C = torch.zeros_like(self.lnS2)
+        self.varD = torch.zeros_like(self.lnS2)
+        self.varCD = torch.zeros_like(self.lnS2)
+        self.discr = torch.zeros_like(self.lnS2)
+        self.filmD = torch.zeros(3, H, W, dtype=dt, device=dev)
+
+    # -- helpers ---------------------------------------------------------------
+    def moment(self, k: int, q: int) -> torch.Tensor:
+        return self.stats[k, q]
+
+    def reset(self) -> None:
+        self.n.zero_()
+        self.stats.zero_()
+        self.gmean.zero_()
+
+    def _gbuffers(self, specs: Sequence[GBufferSpec]) -> L.GBuffers:
+        g = L.GBuffers()
+        g.count = len(specs)
+        for i, s in enumerate(specs):
+            if s.first + s.channels > self.G:
+                raise ValueError("G-buffer spec outside the feature channels")
+            g.planes[i] = _ptr(self.gmean[s.first])
+            g.channels[i] = s.channels
+            g.dr_factor[i] = -0.5 / (s.sigma * s.sigma)
+        return g
+
+    # -- stage 1 -----------------------------------------------------------------
+    def accumulate(self, samples: torch.Tensor, count: Optional[torch.Tensor] = None, mode: int = L.ACC_EXACT,
+                   stream=None) -> None:
+        """StatTile::AddTransformSample* over sample planes [S, 5+G, H, W] (float32)."""
+        if samples.dtype != torch.float32 or not samples.is_contiguous():
+            raise ValueError("samples must be contiguous float32 [S, 5+G, H, W]")
+        S = samples.shape[0]
+        if samples.shape[1:] != (5 + self.G, self.H, self.W):
+            raise ValueError(f"samples shape {tuple(samples.shape)} does not match the buffers")
+        a = L.AccumulateArgs()
+        a.width, a.height, a.n_samples, a.n_features = self.W, self.H, S, self.G
+        a.samples, a.count = _ptr(samples), _ptr(count)
+        a.n_transforms = self.K
+        for k, (kind, lam) in enumerate(self.transforms):
+            a.transforms[k].kind = kind
+            a.transforms[k].lambda_ = lam
+        a.max_moment, a.precision, a.mode = self.max_moment, self.precision, int(mode)
+        a.n, a.stats, a.gmean = _ptr(self.n), _ptr(self.stats), _ptr(self.gmean)
+        L.call("stater_accumulate", C.byref(a), _stream_ptr(stream))
+
+    # -- stage 2 -----------------------------------------------------------------
+    def denoise_vars(self, radius: int = 10, filter_sd: float = 10.0, var_z: float = 2.80703,
+                     gbuffers: Sequence[GBufferSpec] = GBUFFERS_ALBEDO_NORMAL,
+                     m2c_in: Optional[torch.Tensor] = None, stream=None) -> None:
+        a = L.DenoiseVarsArgs()
+        a.n_buffers, a.width, a.height = self.K, self.W, self.H
+        a.filter_radius, a.ds_factor, a.var_z = int(radius), -0.5 / (filter_sd * filter_sd), float(var_z)
+        a.max_moment, a.precision, a.n = self.max_moment, self.precision, _ptr(self.n)
+        for k in range(self.K):
+            a.m2[k] = _ptr(self.stats[k, L.Q_M2])
+            a.m3[k] = _ptr(self.stats[k, L.Q_M3])
+            a.m4[k] = _ptr(self.stats[k, L.Q_M4])
+            a.c2X[k] = _ptr(self.stats[k, L.Q_C2X])
+            a.c2Y[k] = _ptr(self.stats[k, L.Q_C2Y])
+            a.jb[k] = _ptr(self.jb[k])
+            a.lnS2[k] = _ptr(self.lnS2[k])
+            a.se2[k] = _ptr(self.se2[k])
+            a.m2C[k] = _ptr(self.m2C[k])
+            a.varD[k] = _ptr(self.varD[k])
+            a.varCD[k] = _ptr(self.varCD[k])
+        a.m2C_in = _ptr(m2c_in)
+        a.gbuffers = self._gbuffers(gbuffers)
+        L.call("stater_denoise_vars", C.byref(a), _stream_ptr(stream))
+
+    def denoise_film(self, radius: int = 10, filter_sd: float = 10.0, alpha: float = 0.01,
+                     gbuffers: Sequence[GBufferSpec] = GBUFFERS_ALBEDO_NORMAL, mt_mode: int = L.MT_ALL,
+                     use_levc: bool = False, film: Optional[torch.Tensor] = None,
+                     accept_bits: Optional[torch.Tensor] = None, stream=None) -> None:
+        a = L.DenoiseFilmArgs()
+        a.n_buffers, a.width, a.height = self.K, self.W, self.H
+        a.filter_radius, a.ds_factor, a.alpha = int(radius), -0.5 / (filter_sd * filter_sd), float(alpha)
+        a.mt_mode, a.use_levc, a.precision = int(mt_mode), int(bool(use_levc)), self.precision
+        a.n = _ptr(self.n)
+        a.film = _ptr(film if film is not None else self.stats[0, L.Q_MEAN])
+        for k in range(self.K):
+            a.mean[k] = _ptr(self.stats[k, L.Q_MEAN])
+            a.varD[k] = _ptr(self.varD[k])
+            a.varCD[k] = _ptr(self.varCD[k])
+            a.jb[k] = _ptr(self.jb[k])
+            a.discr[k] = _ptr(self.discr[k])
+        a.filmD = _ptr(self.filmD)
+        a.accept_bits = _ptr(accept_bits)
+        a.gbuffers = self._gbuffers(gbuffers)
+        L.call("stater_denoise_film", C.byref(a), _stream_ptr(stream))
+
+    def calc_target_spp(self, spp: int, out: torch.Tensor, relative: bool = True, eps: float = 1e-4,
+                        tmin: int = 16, tmax: int = 1024, stream=None) -> None:
+        mean = self.stats[0, L.Q_MEAN] if relative else None
+        L.call("stater_calc_target_spp", self.W, self.H, int(spp), self.precision, _ptr(self.n),
+               _ptr(self.varD[0]), _ptr(mean), float(eps), int(tmin), int(tmax), _ptr(out),
+               _stream_ptr(stream))
+
+
+def bits_words(radius: int) -> int:
+    d = 2 * radius + 1
+    return (d * d + 31) // 32
+
+
+def generate_samples(width: int, height: int, n_samples: int, n_features: int = 7, seed: int = 0,
+                     region: int = 8, mean_mu: float = -1.0, mean_sigma: float = 1.0, noise_sigma: float = 0.5,
+                     firefly_prob: float = 1e-3, firefly_scale: float = 1e3, lev_r2: float = 0.0,
+                     first_index: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None,
+                     device="cuda", stream=None) -> torch.Tensor:
+    """Seeded synthetic sample planes [S, 5+G, H, W] generated on the device."""
+    if out is None:
+        out = torch.empty(n_samples, 5 + n_features, height, width, dtype=torch.float32, device=device)
+    g = L.GenerateArgs()
+    g.width, g.height, g.n_samples, g.n_features = width, height, n_samples, n_features
+    g.seed, g.region = int(seed), int(region)
+    g.mean_mu, g.mean_sigma, g.noise_sigma = mean_mu, mean_sigma, noise_sigma
+    g.firefly_prob, g.firefly_scale, g.lev_r2 = firefly_prob, firefly_scale, lev_r2
+    g.first_index, g.samples = _ptr(first_index), _ptr(out)
+    L.call("stater_generate_samples", C.byref(g), _stream_ptr(stream))
+    return out
+
+
+def merge_tiles(width: int, height: int, bounds: torch.Tensor, records: torch.Tensor, n_sets: int,
+                n: torch.Tensor, stats: torch.Tensor, stream=None) -> None:
+    L.call("stater_merge_tiles", width, height, int(bounds.shape[0]), _ptr(bounds), _ptr(records), int(n_sets),
+           _ptr(n), _ptr(stats), _stream_ptr(stream))
+
+
+def merge_moments(a: StatBuffers, b: StatBuffers, stream=None) -> None:
+    L.call("stater_merge_moments", a.W, a.H, a.K, a.max_moment, a.precision, _ptr(a.n), _ptr(a.stats),
+           _ptr(b.n), _ptr(b.stats), _stream_ptr(stream))
+
+
+def calc_mean_var(width: int, height: int, n: torch.Tensor, m2: torch.Tensor, out: torch.Tensor,
+                  stream=None) -> None:
+    L.call("stater_calc_mean_var", width, height, _ptr(n), _ptr(m2), _ptr(out), _stream_ptr(stream))
+
+
+class LevState:
+    """Per-pixel LEV accumulation state and the regression outputs."""
+
+    def __init__(self, width: int, height: int, n_features: int = 7, precision: int = L.F64, device="cuda"):
+        self.W, self.H, self.G, self.precision = width, height, n_features, precision
+        lib = L.load()
+        ns = lib.stater_lev_state_size(n_features, precision)
+        if ns <= 0:
+            raise ValueError("unsupported number of features for LEV")
+        dt = _dtype(precision)
+        self.state = torch.zeros(ns, height, width, dtype=dt, device=device)
+        self.beta = torch.zeros(3, n_features + 1, height, width, dtype=dt, device=device)
+        self.m2C = torch.zeros(3, height, width, dtype=dt, device=device)
+        self.r2 = torch.zeros(3, height, width, dtype=dt, device=device)
+
+    def accumulate(self, samples: torch.Tensor, count: Optional[torch.Tensor] = None, stream=None) -> None:
+        L.call("stater_lev_accumulate", self.W, self.H, self.G, int(samples.shape[0]), _ptr(samples),
+               _ptr(count), self.precision, _ptr(self.state), _stream_ptr(stream))
+
+    def solve(self, lam: float = 1e-6, stream=None) -> None:
+        L.call("stater_lev_solve", self.W, self.H, self.G, self.precision, _ptr(self.state), float(lam),
+               _ptr(self.beta), _ptr(self.m2C), _ptr(self.r2), _stream_ptr(stream))
+
+
+def setup() -> None:
+    L.call("stater_setup")
+
+
+def tcrit2_table(alpha: float):
+    import numpy as np
+    lib = L.load()
+    n = lib.stater_tcrit_lut_intervals()
+    out = np.zeros(n + 1, dtype=np.float64)
+    L.call("stater_tcrit2_table", float(alpha), out.ctypes.data)
+    return out

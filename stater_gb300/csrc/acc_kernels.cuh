@@ -1,0 +1,177 @@
+// Stage-1 kernels: per-pixel online moments of radiance under K transforms.
+//
+// One thread owns one (pixel, transform) pair: threadIdx.x walks pixels,
+// threadIdx.y is the transform. The K threads of a pixel read the same sample
+// words, so every sample plane is fetched from HBM once and served to the other
+// transforms from L1. Moments live in registers for the whole call and are
+// written back once, so the state crosses HBM twice per call regardless of the
+// number of samples. Sample planes [S][5+G][HW] make every load a coalesced
+// 128-byte row per warp.
+//
+// The update is the reference's (StatTile::AddStatSampleM1..M4C,
+// src/statistics/estimator.h:226-305): n is incremented first, m2 updated
+// before m3 uses it, m4 after m3, c2X/c2Y with the updated mean and the float
+// offset inPxP - 0.5f, m1 += sqrt(d (d - dN)). EXACT divides by n (bitwise the
+// reference's arithmetic when compiled with -fmad=false); FAST multiplies by a
+// reciprocal shared by all moments of the sample.
+#pragma once
+
+#include "common.cuh"
+
+namespace stater {
+
+struct AccParams {
+    size_t HW;
+    int S, G, K, NCH;
+    const float *__restrict__ samples;
+    const int32_t *__restrict__ count;
+    TransformSet ts;
+    int32_t *n;
+    void *stats;
+    void *gmean;
+};
+
+template <typename T, bool FAST>
+__device__ __forceinline__ T acc_transform(int kind, float lambda, T x) {
+    return transform_exact<T>(kind, lambda, x);
+}
+
+template <typename T, bool FAST, int MAXMOM, int MAXF>
+__global__ void __launch_bounds__(256) acc_kernel(AccParams P) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = threadIdx.y;
+    if (p >= P.HW) return;
+    const size_t HW = P.HW;
+    // per-pixel counts beyond the S sample planes are clamped (never read past them)
+    const int cnt = P.count ? min(max(P.count[p], 0), P.S) : P.S;
+    const uint32_t n0 = (uint32_t)P.n[p];
+    T *st = (T *)P.stats;
+    T *gm = (T *)P.gmean;
+
+    T mean[3], m2[3], m3[3], m4[3], cx[3], cy[3], m1[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        mean[c] = st[stat_index(k, STATER_Q_MEAN, c, HW) + p];
+        m2[c] = MAXMOM >= 2 ? st[stat_index(k, STATER_Q_M2, c, HW) + p] : T(0);
+        m3[c] = MAXMOM >= 3 ? st[stat_index(k, STATER_Q_M3, c, HW) + p] : T(0);
+        m4[c] = MAXMOM >= 4 ? st[stat_index(k, STATER_Q_M4, c, HW) + p] : T(0);
+        cx[c] = MAXMOM >= 5 ? st[stat_index(k, STATER_Q_C2X, c, HW) + p] : T(0);
+        cy[c] = MAXMOM >= 5 ? st[stat_index(k, STATER_Q_C2Y, c, HW) + p] : T(0);
+        m1[c] = MAXMOM >= 5 ? st[stat_index(k, STATER_Q_M1, c, HW) + p] : T(0);
+    }
+    T fm[MAXF > 0 ? MAXF : 1];
+#pragma unroll
+    for (int j = 0; j < MAXF; j++) {
+        const int g = k + j * P.K;
+        fm[j] = g < P.G ? gm[(size_t)g * HW + p] : T(0);
+    }
+    const int kind = P.ts.kind[k];
+    const float lam = P.ts.lambda[k];
+    const float *sp = P.samples + p;
+    const size_t sstride = (size_t)P.NCH * HW;
+
+    for (int s = 0; s < cnt; s++, sp += sstride) {
+        const uint32_t nn = n0 + (uint32_t)s + 1u;
+        const T nT = (T)nn;
+        T rn = T(0);
+        if (FAST) rn = T(1) / nT;
+        float raw[3];
+        raw[0] = __ldg(sp);
+        raw[1] = __ldg(sp + HW);
+        raw[2] = __ldg(sp + 2 * HW);
+        float xD = 0.f, yD = 0.f;
+        if (MAXMOM >= 5) {
+            xD = __ldg(sp + 3 * HW) - 0.5f;
+            yD = __ldg(sp + 4 * HW) - 0.5f;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const T x = acc_transform<T, FAST>(kind, lam, (T)raw[c]);
+            const T d = x - mean[c];
+            const T dN = FAST ? d * rn : d / nT;
+            if (MAXMOM <= 1) {
+                mean[c] = mean[c] + dN;
+            } else if (MAXMOM == 2) {
+                mean[c] = mean[c] + dN;
+                m2[c] = m2[c] + d * (d - dN);
+            } else {
+                const T d2 = d * d;
+                const T dN2 = dN * dN;
+                mean[c] = mean[c] + dN;
+                m2[c] = m2[c] + d * (d - dN);
+                m3[c] = m3[c] + ((T)-3.f * dN * m2[c] + d * (d2 - dN2));
+                if (MAXMOM >= 4)
+                    m4[c] = m4[c] + (((T)-4.f * dN * m3[c] - (T)6.f * dN2 * m2[c]) + d * (d * d2 - dN * dN2));
+                if (MAXMOM >= 5) {
+                    cx[c] = cx[c] + (x - mean[c]) * (T)xD;
+                    cy[c] = cy[c] + (x - mean[c]) * (T)yD;
+                    m1[c] = m1[c] + sqrt(d * (d - dN));
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < MAXF; j++) {
+            const int g = k + j * P.K;
+            if (g < P.G) {
+                const T d = (T)__ldg(sp + (size_t)(5 + g) * HW) - fm[j];
+                const T dN = FAST ? d * rn : d / nT;
+                fm[j] = fm[j] + dN;
+            }
+        }
+    }
+
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        st[stat_index(k, STATER_Q_MEAN, c, HW) + p] = mean[c];
+        if (MAXMOM >= 2) st[stat_index(k, STATER_Q_M2, c, HW) + p] = m2[c];
+        if (MAXMOM >= 3) st[stat_index(k, STATER_Q_M3, c, HW) + p] = m3[c];
+        if (MAXMOM >= 4) st[stat_index(k, STATER_Q_M4, c, HW) + p] = m4[c];
+        if (MAXMOM >= 5) {
+            st[stat_index(k, STATER_Q_C2X, c, HW) + p] = cx[c];
+            st[stat_index(k, STATER_Q_C2Y, c, HW) + p] = cy[c];
+            st[stat_index(k, STATER_Q_M1, c, HW) + p] = m1[c];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < MAXF; j++) {
+        const int g = k + j * P.K;
+        if (g < P.G) gm[(size_t)g * HW + p] = fm[j];
+    }
+    if (k == 0) P.n[p] = (int32_t)(n0 + (uint32_t)cnt);
+}
+
+inline int acc_threads_x(int K) {
+    int tx = (256 / K) & ~31;
+    return tx < 32 ? 32 : tx;
+}
+
+template <typename T, bool FAST, int MAXMOM, int MAXF>
+cudaError_t launch_acc_mf(const AccParams &P, cudaStream_t s) {
+    const int tx = acc_threads_x(P.K);
+    dim3 block(tx, P.K);
+    dim3 grid((unsigned)((P.HW + tx - 1) / tx));
+    acc_kernel<T, FAST, MAXMOM, MAXF><<<grid, block, 0, s>>>(P);
+    return cudaGetLastError();
+}
+
+template <typename T, bool FAST, int MAXMOM>
+cudaError_t launch_acc_m(const AccParams &P, cudaStream_t s) {
+    const int per = P.G == 0 ? 0 : (P.G + P.K - 1) / P.K;
+    if (per == 0) return launch_acc_mf<T, FAST, MAXMOM, 0>(P, s);
+    if (per <= 4) return launch_acc_mf<T, FAST, MAXMOM, 4>(P, s);
+    if (per <= 8) return launch_acc_mf<T, FAST, MAXMOM, 8>(P, s);
+    return launch_acc_mf<T, FAST, MAXMOM, 16>(P, s);
+}
+
+template <typename T, bool FAST>
+cudaError_t launch_acc(const AccParams &P, int max_moment, cudaStream_t s) {
+    switch (max_moment) {
+        case 1: return launch_acc_m<T, FAST, 1>(P, s);
+        case 2: return launch_acc_m<T, FAST, 2>(P, s);
+        case 3: return launch_acc_m<T, FAST, 3>(P, s);
+        case 4: return launch_acc_m<T, FAST, 4>(P, s);
+        default: return launch_acc_m<T, FAST, 5>(P, s);
+    }
+}
+
+}  // namespace stater

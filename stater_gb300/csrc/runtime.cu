@@ -1,0 +1,196 @@
+// Library runtime: error reporting, setup, per-device scratch and the cached
+// Student-t critical-value tables. Host code only.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "common.cuh"
+#include "tquantile.h"
+
+namespace stater {
+
+namespace {
+thread_local std::string g_last_error;
+
+struct ScratchBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct LutEntry {
+    float *f32 = nullptr;
+    double *f64 = nullptr;
+};
+
+std::mutex g_mutex;
+std::map<std::tuple<int, cudaStream_t, int>, ScratchBuf> g_scratch;
+std::map<std::pair<int, double>, LutEntry> g_luts;
+std::map<int, int> g_sm_count;
+
+constexpr int kLutIntervals = 1024;
+}  // namespace
+
+stater_status set_error(stater_status s, const std::string &msg) {
+    g_last_error = msg;
+    return s;
+}
+
+stater_status clear_error() {
+    g_last_error.clear();
+    return STATER_OK;
+}
+
+stater_status cuda_status(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return STATER_OK;
+    return set_error(e == cudaErrorMemoryAllocation ? STATER_ERR_NOMEM : STATER_ERR_CUDA,
+                     std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int sm_count() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_mutex);
+    auto it = g_sm_count.find(dev);
+    if (it != g_sm_count.end()) return it->second;
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+    g_sm_count[dev] = n;
+    return n;
+}
+
+void *scratch(int slot, size_t bytes, cudaStream_t stream) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_mutex);
+    ScratchBuf &b = g_scratch[std::make_tuple(dev, stream, slot)];
+    if (b.bytes >= bytes && b.ptr) return b.ptr;
+    if (b.ptr) {
+        // Earlier work on this stream may still read the old buffer.
+        cudaStreamSynchronize(stream);
+        cudaFree(b.ptr);
+        b.ptr = nullptr;
+        b.bytes = 0;
+    }
+    size_t want = bytes < 256 ? 256 : bytes;
+    if (cudaMalloc(&b.ptr, want) != cudaSuccess) {
+        cudaGetLastError();
+        b.ptr = nullptr;
+        return nullptr;
+    }
+    b.bytes = want;
+    return b.ptr;
+}
+
+int tcrit_intervals() { return kLutIntervals; }
+
+const void *tcrit_table_device(double alpha, bool f64, cudaStream_t stream) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_mutex);
+    LutEntry &e = g_luts[std::make_pair(dev, alpha)];
+    if (!e.f64) {
+        std::vector<double> t(kLutIntervals + 1);
+        tcrit2_table(alpha, kLutIntervals, t.data());
+        std::vector<float> tf(t.begin(), t.end());
+        if (cudaMalloc(&e.f64, sizeof(double) * t.size()) != cudaSuccess ||
+            cudaMalloc(&e.f32, sizeof(float) * t.size()) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        cudaMemcpy(e.f64, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(e.f32, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice);
+    }
+    (void)stream;
+    return f64 ? (const void *)e.f64 : (const void *)e.f32;
+}
+
+}  // namespace stater
+
+using namespace stater;
+
+extern "C" {
+
+const char *stater_last_error(void) { return g_last_error.c_str(); }
+
+int32_t stater_abi_version(void) { return STATER_ABI_VERSION; }
+
+stater_status stater_setup(void) {
+    clear_error();
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetDeviceProperties");
+    if (prop.major != 10 || prop.minor != 3)
+        return set_error(STATER_ERR_UNSUPPORTED,
+                         "libstater is built for sm_103a; device reports sm_" +
+                             std::to_string(prop.major) + std::to_string(prop.minor));
+    sm_count();
+    return STATER_OK;
+}
+
+stater_status stater_synchronize(stater_stream stream) {
+    clear_error();
+    return cuda_status(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
+}
+
+void stater_print_macro_configuration(void) {
+    std::printf("==== stater runtime configuration ====\n");
+    std::printf("ABI_VERSION = %d\n", STATER_ABI_VERSION);
+    std::printf("MAX_TRANSFORMS = %d\n", STATER_MAX_TRANSFORMS);
+    std::printf("MAX_GBUFFERS = %d\n", STATER_MAX_GBUFFERS);
+    std::printf("MAX_RADIUS = %d\n", STATER_MAX_RADIUS);
+    std::printf("TCRIT_LUT_INTERVALS = %d\n", kLutIntervals);
+    std::printf("FILM_MULTI_TRANSFORM_MODE = per call (2 = all, 3 = Jarque-Bera select)\n");
+    std::printf("USE_LEVC = per call (use_levc)\n");
+    std::printf("PRECISION = per call (F64 plain form, F32 form)\n");
+    std::printf("==== end ====\n");
+}
+
+stater_status stater_release_cache(void) {
+    clear_error();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceSynchronize();
+    std::lock_guard<std::mutex> lk(g_mutex);
+    for (auto it = g_scratch.begin(); it != g_scratch.end();) {
+        if (std::get<0>(it->first) == dev) {
+            cudaFree(it->second.ptr);
+            it = g_scratch.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    for (auto it = g_luts.begin(); it != g_luts.end();) {
+        if (it->first.first == dev) {
+            cudaFree(it->second.f32);
+            cudaFree(it->second.f64);
+            it = g_luts.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    return STATER_OK;
+}
+
+int32_t stater_tcrit_lut_intervals(void) { return kLutIntervals; }
+
+stater_status stater_tcrit2_table(double alpha, double *table) {
+    clear_error();
+    if (!(alpha > 0.0 && alpha < 1.0) || !table)
+        return set_error(STATER_ERR_INVALID, "stater_tcrit2_table: alpha must be in (0, 1)");
+    tcrit2_table(alpha, kLutIntervals, table);
+    return STATER_OK;
+}
+
+double stater_t_quantile(double p, double df) { return t_quantile(p, df); }
+
+}  // extern "C"

@@ -1,0 +1,119 @@
+// calcTargetSPP (estimator.cpp:498-513 call site): next-round sample budget per
+// pixel. Compiled with -fmad=false. The image-wide sum of the per-pixel error
+// estimates uses a fixed reduction tree (256 threads x 4 values per 1024-entry
+// block: v0+v1+v2+v3 per thread, then pairwise halving 128..1; block sums
+// reduced again the same way), so the result does not depend on scheduling and
+// equals the CPU restatement bit for bit.
+#include <cmath>
+
+#include "common.cuh"
+
+namespace stater {
+namespace {
+
+template <typename T>
+__global__ void tspp_error_kernel(size_t HW, const int32_t *__restrict__ n, const T *__restrict__ varD,
+                                  const T *__restrict__ mean, double eps, double *e) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= HW) return;
+    const int nn = n[p];
+    if (nn < 2) {
+        e[p] = 0.0;
+        return;
+    }
+    const double nd = (double)nn;
+    double acc = 0.0;
+    for (int c = 0; c < 3; c++) {
+        double v = (double)varD[(size_t)c * HW + p] / nd;
+        if (mean) {
+            const double m = (double)mean[(size_t)c * HW + p];
+            v = v / (m * m + eps);
+        }
+        acc = acc + v;
+    }
+    e[p] = acc;
+}
+
+__global__ void tree_block_kernel(const double *__restrict__ in, long long len, double *out) {
+    __shared__ double part[256];
+    const int t = threadIdx.x;
+    const long long base = (long long)blockIdx.x * 1024;
+    double v[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const long long idx = base + t + 256LL * r;
+        v[r] = idx < len ? in[idx] : 0.0;
+    }
+    part[t] = ((v[0] + v[1]) + v[2]) + v[3];
+    __syncthreads();
+    for (int s = 128; s >= 1; s >>= 1) {
+        if (t < s) part[t] = part[t] + part[t + s];
+        __syncthreads();
+    }
+    if (t == 0) out[blockIdx.x] = part[0];
+}
+
+__global__ void tspp_target_kernel(size_t HW, int spp, const int32_t *__restrict__ n, const double *__restrict__ e,
+                                   const double *__restrict__ total_ptr, int tmin, int tmax, int32_t *target) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= HW) return;
+    const double total = *total_ptr;
+    const double budget = (double)spp * (double)HW;
+    double t;
+    if (n[p] < 2)
+        t = (double)tmax;
+    else if (!(total > 0.0))
+        t = (double)spp;
+    else
+        t = rint(budget * e[p] / total);
+    if (t < tmin) t = tmin;
+    if (t > tmax) t = tmax;
+    target[p] = (int32_t)t;
+}
+
+}  // namespace
+}  // namespace stater
+
+using namespace stater;
+
+extern "C" stater_status stater_calc_target_spp(int32_t width, int32_t height, int32_t spp, stater_precision precision,
+                                                const int32_t *n, const void *varD, const void *mean, double eps,
+                                                int32_t tmin, int32_t tmax, int32_t *targetspp, stater_stream stream) {
+    clear_error();
+    if (width <= 0 || height <= 0 || spp < 0 || !n || !varD || !targetspp || tmin < 0 || tmax < tmin ||
+        !(eps >= 0.0))
+        return set_error(STATER_ERR_INVALID, "stater_calc_target_spp: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t HW = (size_t)width * height;
+    const size_t nb1 = (HW + 1023) / 1024;
+    double *e = (double *)scratch(2, sizeof(double) * (HW + 2 * nb1 + 2), s);
+    if (!e) return set_error(STATER_ERR_NOMEM, "stater_calc_target_spp: scratch allocation failed");
+    double *bufA = e + HW, *bufB = bufA + nb1 + 1;
+    const unsigned grid = (unsigned)((HW + 255) / 256);
+    if (precision == STATER_F64)
+        tspp_error_kernel<double><<<grid, 256, 0, s>>>(HW, n, (const double *)varD, (const double *)mean, eps, e);
+    else if (precision == STATER_F32)
+        tspp_error_kernel<float><<<grid, 256, 0, s>>>(HW, n, (const float *)varD, (const float *)mean, eps, e);
+    else
+        return set_error(STATER_ERR_INVALID, "stater_calc_target_spp: bad precision");
+    STATER_CHECK_LAUNCH("tspp_error_kernel");
+    const double *cur = e;
+    long long len = (long long)HW;
+    double *dst = bufA;
+    if (len == 1) {
+        cudaError_t ce = cudaMemcpyAsync(bufA, e, sizeof(double), cudaMemcpyDeviceToDevice, s);
+        if (ce != cudaSuccess) return cuda_status(ce, "stater_calc_target_spp copy");
+        cur = bufA;
+    }
+    while (len > 1) {
+        const long long nb = (len + 1023) / 1024;
+        tree_block_kernel<<<(unsigned)nb, 256, 0, s>>>(cur, len, dst);
+        STATER_CHECK_LAUNCH("tree_block_kernel");
+        cur = dst;
+        dst = (dst == bufA) ? bufB : bufA;
+        len = nb;
+    }
+    tspp_target_kernel<<<grid, 256, 0, s>>>(HW, spp, n, e, cur, tmin, tmax, targetspp);
+    STATER_CHECK_LAUNCH("tspp_target_kernel");
+    return STATER_OK;
+}
