@@ -411,7 +411,13 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--width", type=int, default=None, help="smaller image for profiling captures")
+    ap.add_argument("--height", type=int, default=None)
+    ap.add_argument("--spp", type=int, default=None)
     args = ap.parse_args()
+    for key in ("width", "height", "spp"):
+        if getattr(args, key) is not None:
+            WORKLOAD[key] = getattr(args, key)
     args.warmup = max(args.warmup, 3)
     args.spp_note = f"{WORKLOAD['spp']} spp"
     world = int(os.environ.get("WORLD_SIZE", "1"))
