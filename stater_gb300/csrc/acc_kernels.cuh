@@ -31,9 +31,103 @@ struct AccParams {
     void *gmean;
 };
 
-template <typename T, bool FAST>
-__device__ __forceinline__ T acc_transform(int kind, float lambda, T x) {
-    return transform_exact<T>(kind, lambda, x);
+// Transform of one radiance value. EXACT: the libm-accurate functions (and the
+// reference's (x^l - 1)/l for Box-Cox). FAST (FP32 only): cheaper forms accurate
+// to a few ulp: sqrt via rsqrt, cbrt via exp2/log2 plus one Newton step, Box-Cox
+// via expm1(l ln x)/l (no cancellation for small l); log1p and asinh stay on the
+// accurate library path because their small-argument accuracy matters.
+template <typename T, bool FAST, int KIND>
+__device__ __forceinline__ T acc_transform(float lambda, T x) {
+    if (!FAST || sizeof(T) == 8) {
+        return transform_exact<T>(KIND, lambda, x);
+    } else {
+        const float xf = (float)x;
+        switch (KIND) {
+            case STATER_TK_LOG1P: return (T)log1pf(xf);
+            case STATER_TK_SQRT: return (T)(xf > 0.f ? xf * rsqrtf(xf) : 0.f);
+            case STATER_TK_CBRT: {
+                if (!(xf > 0.f)) return (T)0.f;
+                float y = exp2f(__log2f(xf) * (1.f / 3.f));
+                y = y - (y * y * y - xf) / (3.f * y * y);
+                return (T)y;
+            }
+            case STATER_TK_ASINH: return (T)asinhf(xf);
+            case STATER_TK_BOXCOX:
+                if (lambda == 1.f) return x;
+                return (T)(expm1f(lambda * logf(xf)) / lambda);
+            default: return x;
+        }
+    }
+}
+
+template <typename T, bool FAST, int MAXMOM, int MAXF, int KIND>
+__device__ __forceinline__ void acc_loop(const AccParams &P, size_t p, int k, int cnt, uint32_t n0, float lam,
+                                         T (&mean)[3], T (&m2)[3], T (&m3)[3], T (&m4)[3], T (&cx)[3],
+                                         T (&cy)[3], T (&m1)[3], T (&fm)[MAXF > 0 ? MAXF : 1]) {
+    const size_t HW = P.HW;
+    const float *sp = P.samples + p;
+    const size_t sstride = (size_t)P.NCH * HW;
+    constexpr int NL = MAXMOM >= 5 ? 5 : 3;
+    // Loads of the next sample are issued before the current one is processed.
+    float nxt[NL];
+    if (cnt > 0) {
+#pragma unroll
+        for (int c = 0; c < NL; c++) nxt[c] = __ldg(sp + (size_t)c * HW);
+    }
+    for (int s = 0; s < cnt; s++) {
+        float cur[NL];
+#pragma unroll
+        for (int c = 0; c < NL; c++) cur[c] = nxt[c];
+        const float *spc = sp;
+        sp += sstride;
+        if (s + 1 < cnt) {
+#pragma unroll
+            for (int c = 0; c < NL; c++) nxt[c] = __ldg(sp + (size_t)c * HW);
+        }
+        const uint32_t nn = n0 + (uint32_t)s + 1u;
+        const T nT = (T)nn;
+        T rn = T(0);
+        if (FAST) rn = T(1) / nT;
+        float xD = 0.f, yD = 0.f;
+        if (MAXMOM >= 5) {
+            xD = cur[3] - 0.5f;
+            yD = cur[4] - 0.5f;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const T x = acc_transform<T, FAST, KIND>(lam, (T)cur[c]);
+            const T d = x - mean[c];
+            const T dN = FAST ? d * rn : d / nT;
+            if (MAXMOM <= 1) {
+                mean[c] = mean[c] + dN;
+            } else if (MAXMOM == 2) {
+                mean[c] = mean[c] + dN;
+                m2[c] = m2[c] + d * (d - dN);
+            } else {
+                const T d2 = d * d;
+                const T dN2 = dN * dN;
+                mean[c] = mean[c] + dN;
+                m2[c] = m2[c] + d * (d - dN);
+                m3[c] = m3[c] + ((T)-3.f * dN * m2[c] + d * (d2 - dN2));
+                if (MAXMOM >= 4)
+                    m4[c] = m4[c] + (((T)-4.f * dN * m3[c] - (T)6.f * dN2 * m2[c]) + d * (d * d2 - dN * dN2));
+                if (MAXMOM >= 5) {
+                    cx[c] = cx[c] + (x - mean[c]) * (T)xD;
+                    cy[c] = cy[c] + (x - mean[c]) * (T)yD;
+                    m1[c] = m1[c] + sqrt(d * (d - dN));
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < MAXF; j++) {
+            const int g = k + j * P.K;
+            if (g < P.G) {
+                const T d = (T)__ldg(spc + (size_t)(5 + g) * HW) - fm[j];
+                const T dN = FAST ? d * rn : d / nT;
+                fm[j] = fm[j] + dN;
+            }
+        }
+    }
 }
 
 template <typename T, bool FAST, int MAXMOM, int MAXF>
@@ -65,59 +159,21 @@ __global__ void __launch_bounds__(256) acc_kernel(AccParams P) {
         const int g = k + j * P.K;
         fm[j] = g < P.G ? gm[(size_t)g * HW + p] : T(0);
     }
-    const int kind = P.ts.kind[k];
     const float lam = P.ts.lambda[k];
-    const float *sp = P.samples + p;
-    const size_t sstride = (size_t)P.NCH * HW;
-
-    for (int s = 0; s < cnt; s++, sp += sstride) {
-        const uint32_t nn = n0 + (uint32_t)s + 1u;
-        const T nT = (T)nn;
-        T rn = T(0);
-        if (FAST) rn = T(1) / nT;
-        float raw[3];
-        raw[0] = __ldg(sp);
-        raw[1] = __ldg(sp + HW);
-        raw[2] = __ldg(sp + 2 * HW);
-        float xD = 0.f, yD = 0.f;
-        if (MAXMOM >= 5) {
-            xD = __ldg(sp + 3 * HW) - 0.5f;
-            yD = __ldg(sp + 4 * HW) - 0.5f;
-        }
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const T x = acc_transform<T, FAST>(kind, lam, (T)raw[c]);
-            const T d = x - mean[c];
-            const T dN = FAST ? d * rn : d / nT;
-            if (MAXMOM <= 1) {
-                mean[c] = mean[c] + dN;
-            } else if (MAXMOM == 2) {
-                mean[c] = mean[c] + dN;
-                m2[c] = m2[c] + d * (d - dN);
-            } else {
-                const T d2 = d * d;
-                const T dN2 = dN * dN;
-                mean[c] = mean[c] + dN;
-                m2[c] = m2[c] + d * (d - dN);
-                m3[c] = m3[c] + ((T)-3.f * dN * m2[c] + d * (d2 - dN2));
-                if (MAXMOM >= 4)
-                    m4[c] = m4[c] + (((T)-4.f * dN * m3[c] - (T)6.f * dN2 * m2[c]) + d * (d * d2 - dN * dN2));
-                if (MAXMOM >= 5) {
-                    cx[c] = cx[c] + (x - mean[c]) * (T)xD;
-                    cy[c] = cy[c] + (x - mean[c]) * (T)yD;
-                    m1[c] = m1[c] + sqrt(d * (d - dN));
-                }
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < MAXF; j++) {
-            const int g = k + j * P.K;
-            if (g < P.G) {
-                const T d = (T)__ldg(sp + (size_t)(5 + g) * HW) - fm[j];
-                const T dN = FAST ? d * rn : d / nT;
-                fm[j] = fm[j] + dN;
-            }
-        }
+    // one specialised sample loop per transform kind (warp-uniform: k = threadIdx.y)
+    switch (P.ts.kind[k]) {
+#define STATER_ACC_CASE(KD)                                                                                   \
+    case KD:                                                                                                  \
+        acc_loop<T, FAST, MAXMOM, MAXF, KD>(P, p, k, cnt, n0, lam, mean, m2, m3, m4, cx, cy, m1, fm);          \
+        break;
+        STATER_ACC_CASE(STATER_TK_LOG1P)
+        STATER_ACC_CASE(STATER_TK_SQRT)
+        STATER_ACC_CASE(STATER_TK_CBRT)
+        STATER_ACC_CASE(STATER_TK_ASINH)
+        STATER_ACC_CASE(STATER_TK_BOXCOX)
+        default: acc_loop<T, FAST, MAXMOM, MAXF, STATER_TK_IDENTITY>(P, p, k, cnt, n0, lam, mean, m2, m3, m4, cx,
+                                                                     cy, m1, fm);
+#undef STATER_ACC_CASE
     }
 
 #pragma unroll

@@ -24,7 +24,7 @@ namespace stater {
 
 namespace {
 
-constexpr int kTX = 16;
+constexpr int kTX2 = 32;
 constexpr int kMaxFeatCh = 24;
 constexpr int kDfMax = 4096;
 constexpr float kLog2e = 1.4426950408889634f;
@@ -32,7 +32,7 @@ constexpr float kLog2e = 1.4426950408889634f;
 struct FeatSet {
     int nch;
     const float *plane[kMaxFeatCh];
-    float scale[kMaxFeatCh];  // dr * log2(e) of the owning G-buffer
+    float mul[kMaxFeatCh];    // sqrt(-dr log2 e) of the owning G-buffer (dr <= 0)
 };
 
 bool make_featset(FeatSet &f, const stater_gbuffers &g, size_t HW) {
@@ -43,7 +43,8 @@ bool make_featset(FeatSet &f, const stater_gbuffers &g, size_t HW) {
         for (int c = 0; c < g.channels[i]; c++) {
             if (f.nch >= kMaxFeatCh) return false;
             f.plane[f.nch] = (const float *)g.planes[i] + (size_t)c * HW;
-            f.scale[f.nch] = g.dr_factor[i] * kLog2e;
+            if (!(g.dr_factor[i] <= 0.f)) return false;
+            f.mul[f.nch] = sqrtf(-g.dr_factor[i] * kLog2e);
             f.nch++;
         }
     }
@@ -140,126 +141,180 @@ __global__ void vars_stats_f32(FastVars P) {
     P.jb[k][p] = nn < 2 ? 0.f : jbsum;
 }
 
-// Stages the halo of `src` ((TX+2R) x (TY+2R) around the tile) into dst;
-// out-of-image entries get `fill`.
-__device__ __forceinline__ void load_halo(float *dst, const float *__restrict__ src, int W, int H, int x0,
-                                          int y0, int R, int hw, int hh, float fill) {
+__device__ __forceinline__ void load_penalty(float *dst, const int32_t *__restrict__ n, int W, int H, int x0,
+                                             int y0, int R, int hw, int hh) {
     const int A = hw * hh;
     for (int idx = threadIdx.x; idx < A; idx += blockDim.x) {
         const int hy = idx / hw, hx = idx - hy * hw;
         const int gx = x0 - R + hx, gy = y0 - R + hy;
-        dst[idx] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? __ldg(src + (size_t)gy * W + gx) : fill;
+        bool ok = false;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) ok = __ldg(n + (size_t)gy * W + gx) >= 2;
+        dst[idx] = ok ? 0.f : -INFINITY;
     }
 }
 
-__device__ __forceinline__ void load_valid(int *dst, const int32_t *__restrict__ n, int W, int H, int x0, int y0,
-                                           int R, int hw, int hh) {
+// ---------------------------------------------------------------------------
+// Tiles: 32 x 8 output pixels per CTA of 128 threads; a warp covers one
+// 32-pixel row (conflict-free shared-memory rows) and each thread owns two
+// vertically adjacent pixels, so every neighbour row it loads serves both.
+// Feature planes are staged pre-scaled by sqrt(-dr log2 e), so the range
+// weight is exp2(ds log2e |dp|^2 - sum_f (f_i - f_j)^2).
+// ---------------------------------------------------------------------------
+// Preferred tile: RB pixels per thread (vertical) x TR thread rows per CTA.
+#ifndef STATER_TILE_RB
+#define STATER_TILE_RB 1
+#endif
+#ifndef STATER_TILE_TR
+#define STATER_TILE_TR 8
+#endif
+
+__device__ __forceinline__ void load_feat_scaled(float *dst, const float *__restrict__ src, float mul, int W, int H,
+                                                 int x0, int y0, int R, int hw, int hh) {
     const int A = hw * hh;
     for (int idx = threadIdx.x; idx < A; idx += blockDim.x) {
         const int hy = idx / hw, hx = idx - hy * hw;
         const int gx = x0 - R + hx, gy = y0 - R + hy;
-        int v = 0;
-        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-            v = __ldg(n + (size_t)gy * W + gx);
-            if (v < 2) v = 0;
+        dst[idx] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? __ldg(src + (size_t)gy * W + gx) * mul : 0.f;
+    }
+}
+
+__device__ __forceinline__ void load_halo_scaled(float *dst, const float *__restrict__ src, float mul, int W, int H,
+                                                 int x0, int y0, int R, int hw, int hh) {
+    const int A = hw * hh;
+    for (int idx = threadIdx.x; idx < A; idx += blockDim.x) {
+        const int hy = idx / hw, hx = idx - hy * hw;
+        const int gx = x0 - R + hx, gy = y0 - R + hy;
+        dst[idx] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? __ldg(src + (size_t)gy * W + gx) * mul : 0.f;
+    }
+}
+
+template <int MF>
+__device__ __forceinline__ float range_arg2(const float (&fi)[MF > 0 ? MF : 1], const float (&fj)[MF > 0 ? MF : 1],
+                                            int nf, float sp) {
+    float a = sp;
+#pragma unroll
+    for (int f = 0; f < MF; f++) {
+        if (f < nf) {
+            const float d = fi[f] - fj[f];
+            a = fmaf(-d, d, a);
         }
-        dst[idx] = v;
     }
+    return a;
 }
 
-// ---------------------------------------------------------------------------
-// Variance filter (varD, varCD).
-// ---------------------------------------------------------------------------
-template <int TY, bool LEVC, int MF>
-__global__ void __launch_bounds__(kTX *TY) vars_filter_f32(FastVars P) {
+template <bool LEVC, int MF, int kRows, int kThreadRows>
+__global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P) {
+    constexpr int kTY = kRows * kThreadRows;
     extern __shared__ float smem[];
-    const int R = P.R, hw = kTX + 2 * R, hh = TY + 2 * R, A = hw * hh;
+    const int R = P.R, hw = kTX2 + 2 * R, hh = kTY + 2 * R, A = hw * hh;
     const int nf = P.feat.nch;
-    int *valid = (int *)smem;
+    float *vpen = smem;  // 0 for a usable neighbour, -inf otherwise (added to the weight exponent)
     float *feat = smem + A;
     float *ln = feat + (size_t)nf * A;
-    float *se = ln + 3 * A;
-    float *sv = se + 3 * A;
+    float *zs = ln + 3 * A;
+    float *sv = zs + 3 * A;
     float *svc = sv + 3 * A;
 
-    const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * TY;
-    const int lx = threadIdx.x % kTX, ly = threadIdx.x / kTX;
-    const int x = x0 + lx, y = y0 + ly;
-    const bool inside = x < P.W && y < P.H;
+    const int x0 = blockIdx.x * kTX2, y0 = blockIdx.y * kTY;
+    const int lx = threadIdx.x % kTX2, tr = threadIdx.x / kTX2;
+    const int x = x0 + lx;
     const size_t HW = (size_t)P.W * P.H;
-    const size_t i = (size_t)y * P.W + x;
-    const int ci = (ly + R) * hw + (lx + R);
 
-    load_valid(valid, P.n, P.W, P.H, x0, y0, R, hw, hh);
-    for (int f = 0; f < nf; f++) load_halo(feat + (size_t)f * A, P.feat.plane[f], P.W, P.H, x0, y0, R, hw, hh, 0.f);
+    load_penalty(vpen, P.n, P.W, P.H, x0, y0, R, hw, hh);
+    for (int f = 0; f < nf; f++)
+        load_feat_scaled(feat + (size_t)f * A, P.feat.plane[f], P.feat.mul[f], P.W, P.H, x0, y0, R, hw, hh);
     __syncthreads();
-    float fi[MF > 0 ? MF : 1];
+
+    int ci[kRows];
+    bool vi[kRows], in[kRows];
+    size_t gi[kRows];
+    float fi[kRows][MF > 0 ? MF : 1];
 #pragma unroll
-    for (int f = 0; f < MF; f++) fi[f] = f < nf ? feat[(size_t)f * A + ci] : 0.f;
-    const bool vi = inside && valid[ci] != 0;
+    for (int q = 0; q < kRows; q++) {
+        const int ly = tr * kRows + q, y = y0 + ly;
+        in[q] = x < P.W && y < P.H;
+        gi[q] = (size_t)y * P.W + x;
+        ci[q] = (ly + R) * hw + (lx + R);
+        vi[q] = in[q] && vpen[ci[q]] == 0.f;
+#pragma unroll
+        for (int f = 0; f < MF; f++) fi[q][f] = f < nf ? feat[(size_t)f * A + ci[q]] : 0.f;
+    }
 
     for (int k = 0; k < P.K; k++) {
         __syncthreads();
         for (int c = 0; c < 3; c++) {
             const size_t off = ((size_t)k * 3 + c) * HW;
-            load_halo(ln + c * A, P.lnS2[k] + (size_t)c * HW, P.W, P.H, x0, y0, R, hw, hh, 0.f);
-            load_halo(se + c * A, P.se2[k] + (size_t)c * HW, P.W, P.H, x0, y0, R, hw, hh, 0.f);
-            load_halo(sv + c * A, P.s2 + off, P.W, P.H, x0, y0, R, hw, hh, 0.f);
-            if (LEVC) load_halo(svc + c * A, P.s2c + off, P.W, P.H, x0, y0, R, hw, hh, 0.f);
+            load_halo_scaled(ln + c * A, P.lnS2[k] + (size_t)c * HW, 1.f, P.W, P.H, x0, y0, R, hw, hh);
+            load_halo_scaled(zs + c * A, P.se2[k] + (size_t)c * HW, P.z2, P.W, P.H, x0, y0, R, hw, hh);
+            load_halo_scaled(sv + c * A, P.s2 + off, 1.f, P.W, P.H, x0, y0, R, hw, hh);
+            if (LEVC) load_halo_scaled(svc + c * A, P.s2c + off, 1.f, P.W, P.H, x0, y0, R, hw, hh);
         }
         __syncthreads();
-        if (!inside) continue;
-        if (!vi) {
-            for (int c = 0; c < 3; c++) {
-                P.varD[k][(size_t)c * HW + i] = 0.f;
-                P.varCD[k][(size_t)c * HW + i] = 0.f;
-            }
-            continue;
-        }
-        float li[3], si[3], aw[3] = {0.f, 0.f, 0.f}, av[3] = {0.f, 0.f, 0.f}, avc[3] = {0.f, 0.f, 0.f};
+        float li[kRows][3], zi[kRows][3], aw[kRows][3], av[kRows][3], avc[kRows][3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            li[c] = ln[c * A + ci];
-            si[c] = se[c * A + ci];
-        }
-        for (int dy = -R; dy <= R; dy++) {
-            const int row = (ly + R + dy) * hw + lx + R;
-            const float sdy = P.ds2 * (float)(dy * dy);
+        for (int q = 0; q < kRows; q++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                li[q][c] = ln[c * A + ci[q]];
+                zi[q][c] = zs[c * A + ci[q]];
+                aw[q][c] = av[q][c] = avc[q][c] = 0.f;
+            }
+        // halo row of pixel q at offset dy is (tr*kRows + q + R + dy); walk rows r relative to pixel 0.
+        for (int r = -R; r <= R + kRows - 1; r++) {
+            const int row = (tr * kRows + R + r) * hw + lx + R;
+            float spq[kRows];
+            bool use[kRows];
+#pragma unroll
+            for (int q = 0; q < kRows; q++) {
+                const int dy = r - q;
+                use[q] = vi[q] && dy >= -R && dy <= R;
+                spq[q] = P.ds2 * (float)(dy * dy);
+            }
+#pragma unroll 4
             for (int dx = -R; dx <= R; dx++) {
                 const int h = row + dx;
-                if (valid[h] == 0) continue;
-                float arg = fmaf(P.ds2, (float)(dx * dx), sdy);
+                const float pen = vpen[h];
+                float fj[MF > 0 ? MF : 1];
 #pragma unroll
-                for (int f = 0; f < MF; f++) {
-                    if (f < nf) {
-                        const float d = fi[f] - feat[(size_t)f * A + h];
-                        arg = fmaf(P.feat.scale[f] * d, d, arg);
-                    }
-                }
-                const float w = exp2f(arg);
+                for (int f = 0; f < MF; f++) fj[f] = f < nf ? feat[(size_t)f * A + h] : 0.f;
+                float lj[3], zj[3], vj[3], vcj[3];
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    const float dl = li[c] - ln[c * A + h];
-                    if (dl * dl <= P.z2 * (si[c] + se[c * A + h])) {
-                        aw[c] += w;
-                        av[c] = fmaf(w, sv[c * A + h], av[c]);
-                        if (LEVC) avc[c] = fmaf(w, svc[c * A + h], avc[c]);
+                    lj[c] = ln[c * A + h];
+                    zj[c] = zs[c * A + h];
+                    vj[c] = sv[c * A + h];
+                    vcj[c] = LEVC ? svc[c * A + h] : 0.f;
+                }
+                const float dxs = fmaf(P.ds2, (float)(dx * dx), pen);
+#pragma unroll
+                for (int q = 0; q < kRows; q++) {
+                    if (!use[q]) continue;
+                    const float w = exp2f(range_arg2<MF>(fi[q], fj, nf, spq[q] + dxs));
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float dl = li[q][c] - lj[c];
+                        const float t = fmaf(-dl, dl, zi[q][c] + zj[c]);
+                        const float m = t >= 0.f ? w : 0.f;
+                        aw[q][c] += m;
+                        av[q][c] = fmaf(m, vj[c], av[q][c]);
+                        if (LEVC) avc[q][c] = fmaf(m, vcj[c], avc[q][c]);
                     }
                 }
             }
         }
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const float vd = av[c] / aw[c];
-            P.varD[k][(size_t)c * HW + i] = vd;
-            P.varCD[k][(size_t)c * HW + i] = LEVC ? avc[c] / aw[c] : vd;
+        for (int q = 0; q < kRows; q++) {
+            if (!in[q]) continue;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const float vd = vi[q] ? av[q][c] / aw[q][c] : 0.f;
+                P.varD[k][(size_t)c * HW + gi[q]] = vd;
+                P.varCD[k][(size_t)c * HW + gi[q]] = vi[q] ? (LEVC ? avc[q][c] / aw[q][c] : vd) : 0.f;
+            }
         }
     }
 }
 
-// ---------------------------------------------------------------------------
-// Welch discriminator and the film filter.
-// ---------------------------------------------------------------------------
 __global__ void film_discr_f32(FastFilm P) {
     const size_t HW = (size_t)P.W * P.H;
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -309,42 +364,91 @@ __device__ __noinline__ int welch_exact(float diff, float di, float dj, int ni, 
     return diff * diff <= t2 * s;
 }
 
-template <int TY, int MF>
-__global__ void __launch_bounds__(kTX *TY) film_filter_f32(FastFilm P) {
+// Mask layout: per pixel, per window row, ceil((2R+1)/32) words: bit dx+R of
+// row dy+R is set while the neighbour is still accepted.
+template <int MF, int kRows, int kThreadRows>
+__global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P) {
+    constexpr int kTY = kRows * kThreadRows;
+    constexpr int kThreads = kTX2 * kThreadRows;
     extern __shared__ float smem[];
-    constexpr int NT = kTX * TY;
-    const int R = P.R, D = 2 * R + 1, words = (D * D + 31) / 32;
-    const int hw = kTX + 2 * R, hh = TY + 2 * R, A = hw * hh;
+    const int R = P.R, D = 2 * R + 1, wpr = (D + 31) / 32, fwords = (D * D + 31) / 32;
+    const int hw = kTX2 + 2 * R, hh = kTY + 2 * R, A = hw * hh;
     const int nf = P.feat.nch;
-    uint32_t *mask = (uint32_t *)smem;                 // [words][NT]
-    int *nval = (int *)(mask + (size_t)words * NT);    // [A]
-    float *feat = (float *)(nval + A);                 // [nf][A]
-    float *mu = feat + (size_t)nf * A;                 // [3][A] (film in the last pass)
-    float *dd = mu + 3 * A;                            // [3][A]
-
-    const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * TY;
     const int t = threadIdx.x;
-    const int lx = t % kTX, ly = t / kTX;
-    const int x = x0 + lx, y = y0 + ly;
-    const bool inside = x < P.W && y < P.H;
-    const size_t HW = (size_t)P.W * P.H;
-    const size_t i = (size_t)y * P.W + x;
-    const int ci = (ly + R) * hw + (lx + R);
+    uint32_t *mask = (uint32_t *)smem;                          // [kRows][D][wpr][kThreads]
+    int *nval = (int *)(mask + (size_t)kRows * D * wpr * kThreads);  // [A]
+    float *feat = (float *)(nval + A);                          // [nf][A]
+    float *mu = feat + (size_t)nf * A;                          // [3][A] (film in the last pass)
+    float *dd = mu + 3 * A;                                     // [3][A]
+    __shared__ int s_nmin, s_nmax;
 
-    for (int w = 0; w < words; w++) mask[(size_t)w * NT + t] = 0xFFFFFFFFu;
-    load_valid(nval, P.n, P.W, P.H, x0, y0, R, hw, hh);
-    for (int f = 0; f < nf; f++) load_halo(feat + (size_t)f * A, P.feat.plane[f], P.W, P.H, x0, y0, R, hw, hh, 0.f);
+    const int x0 = blockIdx.x * kTX2, y0 = blockIdx.y * kTY;
+    const int lx = t % kTX2, tr = t / kTX2;
+    const int x = x0 + lx;
+    const size_t HW = (size_t)P.W * P.H;
+    auto MASK = [&](int q, int row, int w) -> uint32_t & {
+        return mask[(((size_t)q * D + row) * wpr + w) * kThreads + t];
+    };
+
+    if (t == 0) {
+        s_nmin = 0x7fffffff;
+        s_nmax = 0;
+    }
+    for (int q = 0; q < kRows; q++)
+        for (int row = 0; row < D; row++)
+            for (int w = 0; w < wpr; w++) MASK(q, row, w) = 0xFFFFFFFFu;
     __syncthreads();
-    const int ni = inside ? nval[ci] : 0;
-    int ksel = -1;
-    if (inside && P.mt_mode == STATER_MT_JB && ni >= 2) {
-        ksel = 0;
-        float best = P.jb[0][i];
-        for (int k = 1; k < P.K; k++) {
-            const float v = P.jb[k][i];
-            if (v < best) {
-                best = v;
-                ksel = k;
+    {
+        int lmin = 0x7fffffff, lmax = 0;
+        for (int idx = t; idx < A; idx += blockDim.x) {
+            const int hy = idx / hw, hx = idx - hy * hw;
+            const int gx = x0 - R + hx, gy = y0 - R + hy;
+            int v = 0;
+            if (gx >= 0 && gx < P.W && gy >= 0 && gy < P.H) {
+                v = __ldg(P.n + (size_t)gy * P.W + gx);
+                if (v < 2) v = 0;
+            }
+            nval[idx] = v;
+            if (v >= 2) {
+                lmin = min(lmin, v);
+                lmax = max(lmax, v);
+            }
+        }
+        atomicMin(&s_nmin, lmin);
+        atomicMax(&s_nmax, lmax);
+    }
+    for (int f = 0; f < nf; f++)
+        load_feat_scaled(feat + (size_t)f * A, P.feat.plane[f], P.feat.mul[f], P.W, P.H, x0, y0, R, hw, hh);
+    __syncthreads();
+    // All valid n in the halo equal: the df bounds are the same for every pair.
+    const bool uni = s_nmin == s_nmax;
+    float tlo_u = 0.f, thi_u = 0.f;
+    if (uni) {
+        const int dfl = 2 * s_nmin - 2, dfh = s_nmin - 1;
+        tlo_u = dfl > kDfMax ? P.z2lo : __ldg(P.tlo + dfl);
+        thi_u = __ldg(P.thi + (dfh > kDfMax ? kDfMax : dfh));
+    }
+
+    int ci[kRows], ni[kRows], ksel[kRows];
+    bool in[kRows];
+    size_t gi[kRows];
+#pragma unroll
+    for (int q = 0; q < kRows; q++) {
+        const int ly = tr * kRows + q, y = y0 + ly;
+        in[q] = x < P.W && y < P.H;
+        gi[q] = (size_t)y * P.W + x;
+        ci[q] = (ly + R) * hw + (lx + R);
+        ni[q] = in[q] ? nval[ci[q]] : 0;
+        ksel[q] = -1;
+        if (in[q] && P.mt_mode == STATER_MT_JB && ni[q] >= 2) {
+            ksel[q] = 0;
+            float best = P.jb[0][gi[q]];
+            for (int k = 1; k < P.K; k++) {
+                const float v = P.jb[k][gi[q]];
+                if (v < best) {
+                    best = v;
+                    ksel[q] = k;
+                }
             }
         }
     }
@@ -353,103 +457,150 @@ __global__ void __launch_bounds__(kTX *TY) film_filter_f32(FastFilm P) {
         __syncthreads();
         const float *mean = k == 0 ? P.film : P.mean[k];
         for (int c = 0; c < 3; c++) {
-            load_halo(mu + c * A, mean + (size_t)c * HW, P.W, P.H, x0, y0, R, hw, hh, 0.f);
-            load_halo(dd + c * A, P.discr[k] + (size_t)c * HW, P.W, P.H, x0, y0, R, hw, hh, 0.f);
+            load_halo_scaled(mu + c * A, mean + (size_t)c * HW, 1.f, P.W, P.H, x0, y0, R, hw, hh);
+            load_halo_scaled(dd + c * A, P.discr[k] + (size_t)c * HW, 1.f, P.W, P.H, x0, y0, R, hw, hh);
         }
         __syncthreads();
-        if (!inside) continue;
-        if (ni < 2) {
-            if (P.bits)
-                for (int w = 0; w < words; w++) P.bits[(i * P.K + k) * (size_t)words + w] = 0u;
-            continue;
-        }
-        float mi[3], di[3];
+        float mi[kRows][3], di[kRows][3];
+        bool act[kRows], andm[kRows];
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            mi[c] = mu[c * A + ci];
-            di[c] = dd[c * A + ci];
+        for (int q = 0; q < kRows; q++) {
+            act[q] = in[q] && ni[q] >= 2;
+            andm[q] = ksel[q] < 0 || ksel[q] == k;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                mi[q][c] = mu[c * A + ci[q]];
+                di[q][c] = dd[c * A + ci[q]];
+            }
+            if (P.bits && in[q])
+                for (int w = 0; w < fwords; w++) P.bits[(gi[q] * P.K + k) * (size_t)fwords + w] = 0u;
         }
-        const bool and_into_mask = ksel < 0 || ksel == k;
-        uint32_t cur = 0u;
-        int bit = 0, word = 0;
-        for (int dy = -R; dy <= R; dy++) {
-            const int row = (ly + R + dy) * hw + lx + R;
-            for (int dx = -R; dx <= R; dx++, bit++) {
+        // Only the transforms that feed the mask may skip already rejected pairs.
+        const bool skip_rejected = (P.bits == nullptr) && P.mt_mode == STATER_MT_ALL && k > 0;
+        for (int r = -R; r <= R + kRows - 1; r++) {
+            const int row = (tr * kRows + R + r) * hw + lx + R;
+            bool use[kRows];
+            uint32_t prev[kRows][2], cur[kRows][2];
+#pragma unroll
+            for (int q = 0; q < kRows; q++) {
+                const int dy = r - q;
+                use[q] = act[q] && dy >= -R && dy <= R;
+                cur[q][0] = cur[q][1] = 0u;
+                prev[q][0] = prev[q][1] = 0xFFFFFFFFu;
+                if (use[q] && skip_rejected) {
+                    prev[q][0] = MASK(q, dy + R, 0);
+                    if (wpr > 1) prev[q][1] = MASK(q, dy + R, 1);
+                }
+            }
+#pragma unroll 2
+            for (int dx = -R; dx <= R; dx++) {
                 const int h = row + dx;
                 const int nj = nval[h];
-                int a = 0;
-                if (nj >= 2) {
-                    a = 1;
-                    if (dx != 0 || dy != 0) {
-                        const int dfl = ni + nj - 2;
-                        const int dfh = min(ni, nj) - 1;
-                        const float tlo = dfl > kDfMax ? P.z2lo : __ldg(P.tlo + dfl);
-                        const float thi = __ldg(P.thi + (dfh > kDfMax ? kDfMax : dfh));
+                const int b = dx + R, bw = b >> 5, bb = b & 31;
+                float mj[3], dj[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    mj[c] = mu[c * A + h];
+                    dj[c] = dd[c * A + h];
+                }
+#pragma unroll
+                for (int q = 0; q < kRows; q++) {
+                    if (!use[q]) continue;
+                    float tlo = tlo_u, thi = thi_u;
+                    if (!uni) {
+                        // per-pair bounds (only when n varies inside the halo)
+                        const int njc = max(nj, 2);
+                        const int dfl = ni[q] + njc - 2, dfh = min(ni[q], njc) - 1;
+                        tlo = dfl > kDfMax ? P.z2lo : __ldg(P.tlo + dfl);
+                        thi = __ldg(P.thi + (dfh > kDfMax ? kDfMax : dfh));
+                    }
+                    bool acc = true, amb = false;
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float diff = mi[q][c] - mj[c];
+                        const float s = di[q][c] + dj[c];
+                        const float qq = diff * diff;
+                        const bool pos = s > 0.f;
+                        const bool lo = qq <= tlo * s;
+                        const bool hi = qq > thi * s;
+                        acc = acc && (pos ? !hi : diff == 0.f);
+                        amb = amb || (pos && !lo && !hi);
+                    }
+                    int a = (acc && nj >= 2 && ((prev[q][bw] >> bb) & 1u)) ? 1 : 0;
+                    if (a && amb) {
 #pragma unroll
                         for (int c = 0; c < 3; c++) {
-                            const float dj = dd[c * A + h];
-                            const float diff = mi[c] - mu[c * A + h];
-                            const float s = di[c] + dj;
-                            const float q = diff * diff;
-                            if (!(s > 0.f)) {
-                                if (diff != 0.f) a = 0;
-                            } else if (q <= tlo * s) {
-                            } else if (q > thi * s) {
-                                a = 0;
-                            } else {
-                                a &= welch_exact(diff, di[c], dj, ni, nj, P.lut, P.lut_n);
-                            }
+                            const float diff = mi[q][c] - mj[c];
+                            const float s = di[q][c] + dj[c];
+                            const float qq = diff * diff;
+                            if (s > 0.f && !(qq <= tlo * s) && !(qq > thi * s))
+                                a &= welch_exact(diff, di[q][c], dj[c], ni[q], nj, P.lut, P.lut_n);
                         }
                     }
+                    if (dx == 0 && r == q) a = 1;
+                    cur[q][bw] |= (uint32_t)a << bb;
                 }
-                cur |= (uint32_t)a << (bit & 31);
-                if ((bit & 31) == 31 || bit == D * D - 1) {
-                    if (and_into_mask) mask[(size_t)word * NT + t] &= cur;
-                    if (P.bits) P.bits[(i * P.K + k) * (size_t)words + word] = cur;
-                    cur = 0u;
-                    word++;
+            }
+#pragma unroll
+            for (int q = 0; q < kRows; q++) {
+                if (!use[q]) continue;
+                const int dy = r - q;
+                if (andm[q]) {
+                    MASK(q, dy + R, 0) &= cur[q][0];
+                    if (wpr > 1) MASK(q, dy + R, 1) &= cur[q][1];
+                }
+                if (P.bits) {
+                    uint32_t *fb = P.bits + (gi[q] * P.K + k) * (size_t)fwords;
+                    for (int b = 0; b < D; b++) {
+                        if ((cur[q][b >> 5] >> (b & 31)) & 1u) {
+                            const int fbit = (dy + R) * D + b;
+                            fb[fbit >> 5] |= 1u << (fbit & 31);
+                        }
+                    }
                 }
             }
         }
     }
 
     __syncthreads();
-    for (int c = 0; c < 3; c++) load_halo(mu + c * A, P.film + (size_t)c * HW, P.W, P.H, x0, y0, R, hw, hh, 0.f);
+    for (int c = 0; c < 3; c++) load_halo_scaled(mu + c * A, P.film + (size_t)c * HW, 1.f, P.W, P.H, x0, y0, R, hw, hh);
     __syncthreads();
-    if (!inside) return;
-    if (ni < 2) {
-        for (int c = 0; c < 3; c++) P.filmD[(size_t)c * HW + i] = mu[c * A + ci];
-        return;
-    }
-    float fi[MF > 0 ? MF : 1];
+    float fi[kRows][MF > 0 ? MF : 1];
 #pragma unroll
-    for (int f = 0; f < MF; f++) fi[f] = f < nf ? feat[(size_t)f * A + ci] : 0.f;
-    float sw = 0.f, sf[3] = {0.f, 0.f, 0.f};
-    int bit = 0;
-    for (int dy = -R; dy <= R; dy++) {
-        const int row = (ly + R + dy) * hw + lx + R;
-        const float sdy = P.ds2 * (float)(dy * dy);
-        for (int dx = -R; dx <= R; dx++, bit++) {
-            const uint32_t m = mask[(size_t)(bit >> 5) * NT + t];
-            if (!((m >> (bit & 31)) & 1u)) continue;
-            const int h = row + dx;
-            if (nval[h] < 2) continue;
-            float arg = fmaf(P.ds2, (float)(dx * dx), sdy);
+    for (int q = 0; q < kRows; q++)
 #pragma unroll
-            for (int f = 0; f < MF; f++) {
-                if (f < nf) {
-                    const float d = fi[f] - feat[(size_t)f * A + h];
-                    arg = fmaf(P.feat.scale[f] * d, d, arg);
-                }
-            }
-            const float w = exp2f(arg);
-            sw += w;
+        for (int f = 0; f < MF; f++) fi[q][f] = f < nf ? feat[(size_t)f * A + ci[q]] : 0.f;
 #pragma unroll
-            for (int c = 0; c < 3; c++) sf[c] = fmaf(w, mu[c * A + h], sf[c]);
+    for (int q = 0; q < kRows; q++) {
+        if (!in[q]) continue;
+        if (ni[q] < 2) {
+            for (int c = 0; c < 3; c++) P.filmD[(size_t)c * HW + gi[q]] = mu[c * A + ci[q]];
+            continue;
         }
-    }
+        float sw = 0.f, sf[3] = {0.f, 0.f, 0.f};
+        for (int dy = -R; dy <= R; dy++) {
+            const int row = (tr * kRows + q + R + dy) * hw + lx + R;
+            const float sdy = P.ds2 * (float)(dy * dy);
+            const uint32_t m0 = MASK(q, dy + R, 0);
+            const uint32_t m1 = wpr > 1 ? MASK(q, dy + R, 1) : 0u;
+#pragma unroll 4
+            for (int dx = -R; dx <= R; dx++) {
+                const int b = dx + R;
+                const uint32_t bit = ((b < 32 ? m0 : m1) >> (b & 31)) & 1u;
+                const int h = row + dx;
+                float fj[MF > 0 ? MF : 1];
 #pragma unroll
-    for (int c = 0; c < 3; c++) P.filmD[(size_t)c * HW + i] = sf[c] / sw;
+                for (int f = 0; f < MF; f++) fj[f] = f < nf ? feat[(size_t)f * A + h] : 0.f;
+                const float e = range_arg2<MF>(fi[q], fj, nf, fmaf(P.ds2, (float)(dx * dx), sdy));
+                const float wt = bit ? exp2f(e) : 0.f;
+                sw += wt;
+#pragma unroll
+                for (int c = 0; c < 3; c++) sf[c] = fmaf(wt, mu[c * A + h], sf[c]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) P.filmD[(size_t)c * HW + gi[q]] = sf[c] / sw;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -501,16 +652,19 @@ const DfTables *df_tables(double alpha, cudaStream_t s) {
     return &t;
 }
 
-size_t vars_smem(int R, int TY, int nf) {
-    const size_t A = (size_t)(kTX + 2 * R) * (TY + 2 * R);
-    return A * sizeof(float) * (1 + nf + 12);
+size_t vars_smem(int R, int nf, bool levc, int RB, int TR) {
+    const size_t A = (size_t)(kTX2 + 2 * R) * (RB * TR + 2 * R);
+    return A * sizeof(float) * (1 + nf + 9 + (levc ? 3 : 0));
 }
 
-size_t film_smem(int R, int TY, int nf) {
-    const size_t A = (size_t)(kTX + 2 * R) * (TY + 2 * R);
-    const int D = 2 * R + 1, words = (D * D + 31) / 32;
-    return (size_t)words * kTX * TY * 4 + A * sizeof(float) * (1 + nf + 6);
+size_t film_smem(int R, int nf, int RB, int TR) {
+    const size_t A = (size_t)(kTX2 + 2 * R) * (RB * TR + 2 * R);
+    const int D = 2 * R + 1, wpr = (D + 31) / 32;
+    return (size_t)RB * D * wpr * kTX2 * TR * 4 + A * sizeof(float) * (1 + nf + 6);
 }
+
+// Tile shapes tried in order (the preferred one first, then smaller ones for large radii).
+constexpr int kTileCfg[3][2] = {{STATER_TILE_RB, STATER_TILE_TR}, {1, 4}, {1, 2}};
 
 constexpr size_t kSmemLimit = 227 * 1024;
 
@@ -551,7 +705,7 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
     P.m2c_in = (const float *)a->m2C_in;
     const size_t HW = (size_t)P.W * P.H;
     if (!make_featset(P.feat, a->gbuffers, HW))
-        return set_error(STATER_ERR_INVALID, "stater_denoise_vars: bad gbuffers (at most 24 channels)");
+        return set_error(STATER_ERR_INVALID, "stater_denoise_vars: bad gbuffers (at most 24 channels, dr_factor <= 0)");
     float *scr = (float *)scratch(0, sizeof(float) * 2 * 3 * P.K * HW, s);
     if (!scr) return set_error(STATER_ERR_NOMEM, "stater_denoise_vars: scratch allocation failed");
     P.s2 = scr;
@@ -561,29 +715,29 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
     vars_stats_f32<<<g1, 128, 0, s>>>(P);
     STATER_CHECK_LAUNCH("vars_stats_f32");
 
-    int TY = 16;
-    size_t sm = vars_smem(P.R, TY, P.feat.nch);
-    if (sm > kSmemLimit) {
-        TY = 8;
-        sm = vars_smem(P.R, TY, P.feat.nch);
-    }
-    if (sm > kSmemLimit) return set_error(STATER_ERR_UNSUPPORTED, "stater_denoise_vars: radius too large for FP32 tiles");
-    dim3 grid((P.W + kTX - 1) / kTX, (P.H + TY - 1) / TY);
+    int cfg = 0;
+    while (cfg < 3 && vars_smem(P.R, P.feat.nch, P.levc != 0, kTileCfg[cfg][0], kTileCfg[cfg][1]) > kSmemLimit) cfg++;
+    if (cfg == 3) return set_error(STATER_ERR_UNSUPPORTED, "stater_denoise_vars: radius too large for FP32 tiles");
+    const int RB = kTileCfg[cfg][0], TR = kTileCfg[cfg][1];
+    const size_t sm = vars_smem(P.R, P.feat.nch, P.levc != 0, RB, TR);
+    dim3 grid((P.W + kTX2 - 1) / kTX2, (P.H + RB * TR - 1) / (RB * TR));
     const int mf = mf_bucket(P.feat.nch);
     cudaError_t e = cudaSuccess;
-#define STATER_VARS_LAUNCH(TYV, LV, MFV)                                           \
-    if (TY == TYV && (P.levc != 0) == LV && mf == MFV) {                          \
-        e = set_smem(vars_filter_f32<TYV, LV, MFV>, sm);                          \
-        if (e == cudaSuccess) vars_filter_f32<TYV, LV, MFV><<<grid, kTX * TYV, sm, s>>>(P); \
+#define STATER_VARS_LAUNCH(LV, MFV, RBV, TRV)                                                   \
+    if ((P.levc != 0) == LV && mf == MFV && RB == RBV && TR == TRV) {                           \
+        e = set_smem(vars_filter_f32<LV, MFV, RBV, TRV>, sm);                                   \
+        if (e == cudaSuccess) vars_filter_f32<LV, MFV, RBV, TRV><<<grid, kTX2 * TRV, sm, s>>>(P); \
     }
-#define STATER_VARS_LAUNCH_MF(TYV, LV) \
-    STATER_VARS_LAUNCH(TYV, LV, 0) STATER_VARS_LAUNCH(TYV, LV, 4) STATER_VARS_LAUNCH(TYV, LV, 8) \
-    STATER_VARS_LAUNCH(TYV, LV, 16) STATER_VARS_LAUNCH(TYV, LV, 24)
-    STATER_VARS_LAUNCH_MF(16, true)
-    STATER_VARS_LAUNCH_MF(16, false)
-    STATER_VARS_LAUNCH_MF(8, true)
-    STATER_VARS_LAUNCH_MF(8, false)
-#undef STATER_VARS_LAUNCH_MF
+#define STATER_VARS_LAUNCH_T(RBV, TRV)                                                              \
+    STATER_VARS_LAUNCH(true, 0, RBV, TRV) STATER_VARS_LAUNCH(true, 4, RBV, TRV)                     \
+    STATER_VARS_LAUNCH(true, 8, RBV, TRV) STATER_VARS_LAUNCH(true, 16, RBV, TRV)                    \
+    STATER_VARS_LAUNCH(true, 24, RBV, TRV) STATER_VARS_LAUNCH(false, 0, RBV, TRV)                   \
+    STATER_VARS_LAUNCH(false, 4, RBV, TRV) STATER_VARS_LAUNCH(false, 8, RBV, TRV)                   \
+    STATER_VARS_LAUNCH(false, 16, RBV, TRV) STATER_VARS_LAUNCH(false, 24, RBV, TRV)
+    STATER_VARS_LAUNCH_T(STATER_TILE_RB, STATER_TILE_TR)
+    if (cfg == 1) { STATER_VARS_LAUNCH_T(1, 4) }
+    if (cfg == 2) { STATER_VARS_LAUNCH_T(1, 2) }
+#undef STATER_VARS_LAUNCH_T
 #undef STATER_VARS_LAUNCH
     if (e != cudaSuccess) return cuda_status(e, "vars_filter_f32 smem attribute");
     STATER_CHECK_LAUNCH("vars_filter_f32");
@@ -612,7 +766,7 @@ stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s
     P.bits = a->accept_bits;
     const size_t HW = (size_t)P.W * P.H;
     if (!make_featset(P.feat, a->gbuffers, HW))
-        return set_error(STATER_ERR_INVALID, "stater_denoise_film: bad gbuffers (at most 24 channels)");
+        return set_error(STATER_ERR_INVALID, "stater_denoise_film: bad gbuffers (at most 24 channels, dr_factor <= 0)");
     P.lut = (const float *)tcrit_table_device((double)a->alpha, false, s);
     const DfTables *dt = df_tables((double)a->alpha, s);
     if (!P.lut || !dt) return set_error(STATER_ERR_NOMEM, "stater_denoise_film: table allocation failed");
@@ -624,25 +778,26 @@ stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s
     film_discr_f32<<<g1, 128, 0, s>>>(P);
     STATER_CHECK_LAUNCH("film_discr_f32");
 
-    int TY = 16;
-    size_t sm = film_smem(P.R, TY, P.feat.nch);
-    if (sm > kSmemLimit) {
-        TY = 8;
-        sm = film_smem(P.R, TY, P.feat.nch);
-    }
-    if (sm > kSmemLimit) return set_error(STATER_ERR_UNSUPPORTED, "stater_denoise_film: radius too large for FP32 tiles");
-    dim3 grid((P.W + kTX - 1) / kTX, (P.H + TY - 1) / TY);
+    int cfg = 0;
+    while (cfg < 3 && film_smem(P.R, P.feat.nch, kTileCfg[cfg][0], kTileCfg[cfg][1]) > kSmemLimit) cfg++;
+    if (cfg == 3) return set_error(STATER_ERR_UNSUPPORTED, "stater_denoise_film: radius too large for FP32 tiles");
+    const int RB = kTileCfg[cfg][0], TR = kTileCfg[cfg][1];
+    const size_t sm = film_smem(P.R, P.feat.nch, RB, TR);
+    dim3 grid((P.W + kTX2 - 1) / kTX2, (P.H + RB * TR - 1) / (RB * TR));
     const int mf = mf_bucket(P.feat.nch);
     cudaError_t e = cudaSuccess;
-#define STATER_FILM_LAUNCH(TYV, MFV)                                          \
-    if (TY == TYV && mf == MFV) {                                             \
-        e = set_smem(film_filter_f32<TYV, MFV>, sm);                          \
-        if (e == cudaSuccess) film_filter_f32<TYV, MFV><<<grid, kTX * TYV, sm, s>>>(P); \
+#define STATER_FILM_LAUNCH(MFV, RBV, TRV)                                                    \
+    if (mf == MFV && RB == RBV && TR == TRV) {                                               \
+        e = set_smem(film_filter_f32<MFV, RBV, TRV>, sm);                                    \
+        if (e == cudaSuccess) film_filter_f32<MFV, RBV, TRV><<<grid, kTX2 * TRV, sm, s>>>(P); \
     }
-    STATER_FILM_LAUNCH(16, 0) STATER_FILM_LAUNCH(16, 4) STATER_FILM_LAUNCH(16, 8)
-    STATER_FILM_LAUNCH(16, 16) STATER_FILM_LAUNCH(16, 24)
-    STATER_FILM_LAUNCH(8, 0) STATER_FILM_LAUNCH(8, 4) STATER_FILM_LAUNCH(8, 8)
-    STATER_FILM_LAUNCH(8, 16) STATER_FILM_LAUNCH(8, 24)
+#define STATER_FILM_LAUNCH_T(RBV, TRV)                                                              \
+    STATER_FILM_LAUNCH(0, RBV, TRV) STATER_FILM_LAUNCH(4, RBV, TRV) STATER_FILM_LAUNCH(8, RBV, TRV) \
+    STATER_FILM_LAUNCH(16, RBV, TRV) STATER_FILM_LAUNCH(24, RBV, TRV)
+    STATER_FILM_LAUNCH_T(STATER_TILE_RB, STATER_TILE_TR)
+    if (cfg == 1) { STATER_FILM_LAUNCH_T(1, 4) }
+    if (cfg == 2) { STATER_FILM_LAUNCH_T(1, 2) }
+#undef STATER_FILM_LAUNCH_T
 #undef STATER_FILM_LAUNCH
     if (e != cudaSuccess) return cuda_status(e, "film_filter_f32 smem attribute");
     STATER_CHECK_LAUNCH("film_filter_f32");
