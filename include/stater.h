@@ -258,6 +258,21 @@ stater_status stater_calc_target_spp(int32_t width, int32_t height, int32_t spp,
                                      int32_t tmin, int32_t tmax, int32_t *targetspp,
                                      stater_stream stream);
 
+/* No counterpart in the reference. The same computation as
+ * stater_calc_target_spp for callers that cannot allocate device memory (pool
+ * allocators that own the device, hosts that forbid the device-wide
+ * synchronisation of cudaMalloc/cudaFree): its scratch is a fixed array inside
+ * the library, 2,097,152 pixels at most (W*H above that returns
+ * STATER_ERR_INVALID), about 16.8 MB held on every GPU that loads the library.
+ * The first call on a device resolves the array's address and should come
+ * before any stream capture; calls that overlap on the GPU share the array and
+ * race. */
+stater_status stater_calc_target_spp_noalloc(int32_t width, int32_t height, int32_t spp,
+                                             stater_precision precision, const int32_t *n,
+                                             const void *varD, const void *mean, double eps,
+                                             int32_t tmin, int32_t tmax, int32_t *targetspp,
+                                             stater_stream stream);
+
 /* Estimator::CalcMeanVars / calcMatMeanVar (estimator.cpp:462-496):
  * meanVar = m2 / ((n - 1) * n) in float arithmetic. RGB buffers. */
 stater_status stater_calc_mean_var(int32_t width, int32_t height, const int32_t *n,

@@ -110,6 +110,8 @@ def load() -> C.CDLL:
         "stater_t_quantile": (C.c_double, [C.c_double, C.c_double]),
         "stater_calc_target_spp": (st, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, VP, VP, VP, C.c_double,
                                         C.c_int32, C.c_int32, VP, VP]),
+        "stater_calc_target_spp_noalloc": (st, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, VP, VP, VP,
+                                                C.c_double, C.c_int32, C.c_int32, VP, VP]),
         "stater_calc_mean_var": (st, [C.c_int32, C.c_int32, VP, VP, VP, VP]),
         "stater_lev_state_size": (C.c_int32, [C.c_int32, C.c_int32]),
         "stater_lev_accumulate": (st, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, VP, VP, C.c_int32, VP, VP]),

@@ -5,6 +5,8 @@
 // reduced again the same way), so the result does not depend on scheduling and
 // equals the CPU restatement bit for bit.
 #include <cmath>
+#include <mutex>
+#include <string>
 
 #include "common.cuh"
 
@@ -103,6 +105,106 @@ extern "C" stater_status stater_calc_target_spp(int32_t width, int32_t height, i
     if (len == 1) {
         cudaError_t ce = cudaMemcpyAsync(bufA, e, sizeof(double), cudaMemcpyDeviceToDevice, s);
         if (ce != cudaSuccess) return cuda_status(ce, "stater_calc_target_spp copy");
+        cur = bufA;
+    }
+    while (len > 1) {
+        const long long nb = (len + 1023) / 1024;
+        tree_block_kernel<<<(unsigned)nb, 256, 0, s>>>(cur, len, dst);
+        STATER_CHECK_LAUNCH("tree_block_kernel");
+        cur = dst;
+        dst = (dst == bufA) ? bufB : bufA;
+        len = nb;
+    }
+    tspp_target_kernel<<<grid, 256, 0, s>>>(HW, spp, n, e, cur, tmin, tmax, targetspp);
+    STATER_CHECK_LAUNCH("tspp_target_kernel");
+    return STATER_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of calcTargetSPP.
+//
+// Some callers cannot allocate device memory at the point where they need the
+// next round's sample budget: a renderer whose device memory is carved up by its
+// own pool allocator, or a plugin host that forbids cudaMalloc/cudaFree on its
+// worker threads because those calls synchronise the whole device. For them the
+// scratch of this entry point (the per-pixel error estimates and the reduction
+// partials) lives in a fixed-size array compiled into the library, reserved on
+// every GPU that loads libstater until the process exits.
+//
+// The first call on each device looks up the array's device address
+// (cudaGetSymbolAddress, with that device current); make that first call before
+// any stream capture begins. All calls share the one array, so calls whose work
+// overlaps on the GPU (different streams, no ordering between them) race.
+// ---------------------------------------------------------------------------
+namespace stater {
+namespace {
+
+constexpr size_t kNoAllocMaxPixels = (size_t)1 << 21;  // 2,097,152 pixels: covers 1920x1080
+constexpr size_t kNoAllocBlocks = (kNoAllocMaxPixels + 1023) / 1024;
+constexpr size_t kNoAllocDoubles = kNoAllocMaxPixels + 2 * (kNoAllocBlocks + 1);
+
+// 16.8 MB: errors [kNoAllocMaxPixels], then two ping-pong reduction buffers.
+static __device__ __align__(256) double g_tspp_scratch[kNoAllocDoubles];
+
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[64] = {nullptr};
+
+}  // namespace
+}  // namespace stater
+
+extern "C" stater_status stater_calc_target_spp_noalloc(int32_t width, int32_t height, int32_t spp,
+                                                        stater_precision precision, const int32_t *n,
+                                                        const void *varD, const void *mean, double eps,
+                                                        int32_t tmin, int32_t tmax, int32_t *targetspp,
+                                                        stater_stream stream) {
+    clear_error();
+    if (width <= 0 || height <= 0 || spp < 0 || !n || !varD || !targetspp || tmin < 0 || tmax < tmin ||
+        !(eps >= 0.0))
+        return set_error(STATER_ERR_INVALID, "stater_calc_target_spp_noalloc: bad arguments");
+    const size_t HW = (size_t)width * height;
+    if (HW > kNoAllocMaxPixels)
+        return set_error(STATER_ERR_INVALID,
+                         "stater_calc_target_spp_noalloc: width*height = " + std::to_string(HW) +
+                             " exceeds the fixed scratch of " + std::to_string(kNoAllocMaxPixels) + " pixels");
+    if (precision != STATER_F64 && precision != STATER_F32)
+        return set_error(STATER_ERR_INVALID, "stater_calc_target_spp_noalloc: bad precision");
+    int dev = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess) return cuda_status(ce, "stater_calc_target_spp_noalloc: cudaGetDevice");
+    if (dev < 0 || dev >= 64)
+        return set_error(STATER_ERR_UNSUPPORTED, "stater_calc_target_spp_noalloc: device index above 63");
+    double *scr;
+    {
+        // First call on this device (with it current): resolve the device address
+        // of the array. The host-side symbol is only a stand-in and must never be
+        // handed to a kernel.
+        std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+        if (!g_noalloc_ptr[dev]) {
+            void *p = nullptr;
+            ce = cudaGetSymbolAddress(&p, g_tspp_scratch);
+            if (ce != cudaSuccess) return cuda_status(ce, "stater_calc_target_spp_noalloc: cudaGetSymbolAddress");
+            g_noalloc_ptr[dev] = (double *)p;
+        }
+        scr = g_noalloc_ptr[dev];
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    // Every scratch word this call reads is written earlier in the same call, so
+    // the contents left by a previous call need no clearing.
+    double *e = scr;
+    double *bufA = scr + kNoAllocMaxPixels;
+    double *bufB = bufA + kNoAllocBlocks + 1;
+    const unsigned grid = (unsigned)((HW + 255) / 256);
+    if (precision == STATER_F64)
+        tspp_error_kernel<double><<<grid, 256, 0, s>>>(HW, n, (const double *)varD, (const double *)mean, eps, e);
+    else
+        tspp_error_kernel<float><<<grid, 256, 0, s>>>(HW, n, (const float *)varD, (const float *)mean, eps, e);
+    STATER_CHECK_LAUNCH("tspp_error_kernel");
+    const double *cur = e;
+    long long len = (long long)HW;
+    double *dst = bufA;
+    if (len == 1) {
+        ce = cudaMemcpyAsync(bufA, e, sizeof(double), cudaMemcpyDeviceToDevice, s);
+        if (ce != cudaSuccess) return cuda_status(ce, "stater_calc_target_spp_noalloc copy");
         cur = bufA;
     }
     while (len > 1) {
