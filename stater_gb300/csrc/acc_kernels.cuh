@@ -18,6 +18,10 @@
 
 #include "common.cuh"
 
+#ifndef STATER_ACC_LOOKAHEAD
+#define STATER_ACC_LOOKAHEAD 1
+#endif
+
 namespace stater {
 
 struct AccParams {
@@ -31,11 +35,52 @@ struct AccParams {
     void *gmean;
 };
 
+// Compact FP32 forms used by the FAST mode (few instructions, no slow paths;
+// accurate to a few 1e-7 relative, checked against the FP64 oracle):
+//   log1p: 2 atanh(t), t = x/(2+x), by its Taylor series t + t^3/3 + ... + t^9/9
+//          for x < 1/4 (t < 1/9), else log2(1+x) ln 2 with the hardware log2;
+//   asinh: log1p(x + x^2/(1 + sqrt(1 + x^2))), odd;
+//   cbrt:  2^(log2|x| / 3) refined by one Newton step, odd;
+//   sqrt:  x * rsqrt(x).
+__device__ __forceinline__ float fast_log2(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float fast_exp2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float log1p_compact(float x) {
+    const float t = __fdividef(x, 2.f + x);
+    const float t2 = t * t;
+    float p = fmaf(t2, 1.f / 9.f, 1.f / 7.f);
+    p = fmaf(t2, p, 1.f / 5.f);
+    p = fmaf(t2, p, 1.f / 3.f);
+    p = fmaf(t2, p, 1.f);
+    const float small = 2.f * t * p;
+    const float large = fast_log2(1.f + x) * 0.69314718055994531f;
+    return x < 0.25f ? small : large;
+}
+__device__ __forceinline__ float asinh_compact(float x) {
+    const float a = fabsf(x);
+    const float v = fmaf(a, a, 1.f);
+    const float sq = v * rsqrtf(v);
+    const float r = log1p_compact(a + __fdividef(a * a, 1.f + sq));
+    return copysignf(r, x);
+}
+__device__ __forceinline__ float cbrt_compact(float x) {
+    const float a = fabsf(x);
+    if (!(a > 0.f)) return x;
+    float y = fast_exp2(fast_log2(a) * (1.f / 3.f));
+    y = y - __fdividef(y * y * y - a, 3.f * y * y);
+    return copysignf(y, x);
+}
+
 // Transform of one radiance value. EXACT: the libm-accurate functions (and the
-// reference's (x^l - 1)/l for Box-Cox). FAST (FP32 only): cheaper forms accurate
-// to a few ulp: sqrt via rsqrt, cbrt via exp2/log2 plus one Newton step, Box-Cox
-// via expm1(l ln x)/l (no cancellation for small l); log1p and asinh stay on the
-// accurate library path because their small-argument accuracy matters.
+// reference's (x^l - 1)/l for Box-Cox). FAST (FP32 only): the compact forms
+// above, and Box-Cox as expm1(l ln x)/l (no cancellation for small l).
 template <typename T, bool FAST, int KIND>
 __device__ __forceinline__ T acc_transform(float lambda, T x) {
     if (!FAST || sizeof(T) == 8) {
@@ -43,15 +88,10 @@ __device__ __forceinline__ T acc_transform(float lambda, T x) {
     } else {
         const float xf = (float)x;
         switch (KIND) {
-            case STATER_TK_LOG1P: return (T)log1pf(xf);
-            case STATER_TK_SQRT: return (T)(xf > 0.f ? xf * rsqrtf(xf) : 0.f);
-            case STATER_TK_CBRT: {
-                if (!(xf > 0.f)) return (T)0.f;
-                float y = exp2f(__log2f(xf) * (1.f / 3.f));
-                y = y - (y * y * y - xf) / (3.f * y * y);
-                return (T)y;
-            }
-            case STATER_TK_ASINH: return (T)asinhf(xf);
+            case STATER_TK_LOG1P: return (T)log1p_compact(xf);
+            case STATER_TK_SQRT: return (T)(xf > 0.f ? xf * rsqrtf(xf) : (xf == 0.f ? 0.f : sqrtf(xf)));
+            case STATER_TK_CBRT: return (T)cbrt_compact(xf);
+            case STATER_TK_ASINH: return (T)asinh_compact(xf);
             case STATER_TK_BOXCOX:
                 if (lambda == 1.f) return x;
                 return (T)(expm1f(lambda * logf(xf)) / lambda);
@@ -68,21 +108,28 @@ __device__ __forceinline__ void acc_loop(const AccParams &P, size_t p, int k, in
     const float *sp = P.samples + p;
     const size_t sstride = (size_t)P.NCH * HW;
     constexpr int NL = MAXMOM >= 5 ? 5 : 3;
-    // Loads of the next sample are issued before the current one is processed.
-    float nxt[NL];
-    if (cnt > 0) {
+    // A ring of LA samples stays in flight per thread: the slot just consumed is
+    // refilled with the sample LA steps ahead before the current one is processed.
+    constexpr int LA = STATER_ACC_LOOKAHEAD;
+    float ring[LA][NL];
 #pragma unroll
-        for (int c = 0; c < NL; c++) nxt[c] = __ldg(sp + (size_t)c * HW);
-    }
-    for (int s = 0; s < cnt; s++) {
+    for (int j = 0; j < LA; j++)
+        if (j < cnt) {
+#pragma unroll
+            for (int c = 0; c < NL; c++) ring[j][c] = __ldg(sp + (size_t)j * sstride + (size_t)c * HW);
+        }
+    for (int s0 = 0; s0 < cnt; s0 += LA) {
+#pragma unroll
+    for (int j = 0; j < LA; j++) {
+        const int s = s0 + j;
+        if (s >= cnt) break;
         float cur[NL];
 #pragma unroll
-        for (int c = 0; c < NL; c++) cur[c] = nxt[c];
-        const float *spc = sp;
-        sp += sstride;
-        if (s + 1 < cnt) {
+        for (int c = 0; c < NL; c++) cur[c] = ring[j][c];
+        const float *spc = sp + (size_t)s * sstride;
+        if (s + LA < cnt) {
 #pragma unroll
-            for (int c = 0; c < NL; c++) nxt[c] = __ldg(sp + (size_t)c * HW);
+            for (int c = 0; c < NL; c++) ring[j][c] = __ldg(spc + (size_t)LA * sstride + (size_t)c * HW);
         }
         const uint32_t nn = n0 + (uint32_t)s + 1u;
         const T nT = (T)nn;
@@ -119,14 +166,15 @@ __device__ __forceinline__ void acc_loop(const AccParams &P, size_t p, int k, in
             }
         }
 #pragma unroll
-        for (int j = 0; j < MAXF; j++) {
-            const int g = k + j * P.K;
+        for (int jf = 0; jf < MAXF; jf++) {
+            const int g = k + jf * P.K;
             if (g < P.G) {
-                const T d = (T)__ldg(spc + (size_t)(5 + g) * HW) - fm[j];
+                const T d = (T)__ldg(spc + (size_t)(5 + g) * HW) - fm[jf];
                 const T dN = FAST ? d * rn : d / nT;
-                fm[j] = fm[j] + dN;
+                fm[jf] = fm[jf] + dN;
             }
         }
+    }
     }
 }
 

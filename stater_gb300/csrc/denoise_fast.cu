@@ -189,20 +189,28 @@ __device__ __forceinline__ void load_halo_scaled(float *dst, const float *__rest
 }
 
 template <int MF>
-__device__ __forceinline__ float range_arg2(const float (&fi)[MF > 0 ? MF : 1], const float (&fj)[MF > 0 ? MF : 1],
+__device__ __forceinline__ float range_arg2(const float (&fi)[MF > 0 ? MF : 1], const float *feat, int A, int h,
                                             int nf, float sp) {
     float a = sp;
 #pragma unroll
     for (int f = 0; f < MF; f++) {
         if (f < nf) {
-            const float d = fi[f] - fj[f];
+            const float d = fi[f] - feat[f * A + h];
             a = fmaf(-d, d, a);
         }
     }
     return a;
 }
 
-template <bool LEVC, int MF, int kRows, int kThreadRows>
+__device__ __forceinline__ float fast_exp2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// ZPIX: se2 does not depend on the transform or channel (no kurtosis tracked),
+// so one z^2 se2 plane serves every test.
+template <bool LEVC, bool ZPIX, int MF, int kRows, int kThreadRows>
 __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P) {
     constexpr int kTY = kRows * kThreadRows;
     extern __shared__ float smem[];
@@ -210,10 +218,11 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P)
     const int nf = P.feat.nch;
     float *vpen = smem;  // 0 for a usable neighbour, -inf otherwise (added to the weight exponent)
     float *feat = smem + A;
-    float *ln = feat + (size_t)nf * A;
-    float *zs = ln + 3 * A;
-    float *sv = zs + 3 * A;
-    float *svc = sv + 3 * A;
+    float *zpix = feat + nf * A;            // ZPIX: [A]
+    float *ln = zpix + (ZPIX ? A : 0);      // [3][A]
+    float *zs = ln + 3 * A;                 // !ZPIX: [3][A]
+    float *sv = zs + (ZPIX ? 0 : 3 * A);    // [3][A]
+    float *svc = sv + 3 * A;                // LEVC: [3][A]
 
     const int x0 = blockIdx.x * kTX2, y0 = blockIdx.y * kTY;
     const int lx = threadIdx.x % kTX2, tr = threadIdx.x / kTX2;
@@ -222,13 +231,14 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P)
 
     load_penalty(vpen, P.n, P.W, P.H, x0, y0, R, hw, hh);
     for (int f = 0; f < nf; f++)
-        load_feat_scaled(feat + (size_t)f * A, P.feat.plane[f], P.feat.mul[f], P.W, P.H, x0, y0, R, hw, hh);
+        load_feat_scaled(feat + f * A, P.feat.plane[f], P.feat.mul[f], P.W, P.H, x0, y0, R, hw, hh);
+    if (ZPIX) load_halo_scaled(zpix, P.se2[0], P.z2, P.W, P.H, x0, y0, R, hw, hh);
     __syncthreads();
 
     int ci[kRows];
     bool vi[kRows], in[kRows];
     size_t gi[kRows];
-    float fi[kRows][MF > 0 ? MF : 1];
+    float fi[kRows][MF > 0 ? MF : 1], zpi[kRows];
 #pragma unroll
     for (int q = 0; q < kRows; q++) {
         const int ly = tr * kRows + q, y = y0 + ly;
@@ -236,8 +246,9 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P)
         gi[q] = (size_t)y * P.W + x;
         ci[q] = (ly + R) * hw + (lx + R);
         vi[q] = in[q] && vpen[ci[q]] == 0.f;
+        zpi[q] = ZPIX ? zpix[ci[q]] : 0.f;
 #pragma unroll
-        for (int f = 0; f < MF; f++) fi[q][f] = f < nf ? feat[(size_t)f * A + ci[q]] : 0.f;
+        for (int f = 0; f < MF; f++) fi[q][f] = f < nf ? feat[f * A + ci[q]] : 0.f;
     }
 
     for (int k = 0; k < P.K; k++) {
@@ -245,7 +256,7 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P)
         for (int c = 0; c < 3; c++) {
             const size_t off = ((size_t)k * 3 + c) * HW;
             load_halo_scaled(ln + c * A, P.lnS2[k] + (size_t)c * HW, 1.f, P.W, P.H, x0, y0, R, hw, hh);
-            load_halo_scaled(zs + c * A, P.se2[k] + (size_t)c * HW, P.z2, P.W, P.H, x0, y0, R, hw, hh);
+            if (!ZPIX) load_halo_scaled(zs + c * A, P.se2[k] + (size_t)c * HW, P.z2, P.W, P.H, x0, y0, R, hw, hh);
             load_halo_scaled(sv + c * A, P.s2 + off, 1.f, P.W, P.H, x0, y0, R, hw, hh);
             if (LEVC) load_halo_scaled(svc + c * A, P.s2c + off, 1.f, P.W, P.H, x0, y0, R, hw, hh);
         }
@@ -256,10 +267,9 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P)
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 li[q][c] = ln[c * A + ci[q]];
-                zi[q][c] = zs[c * A + ci[q]];
+                zi[q][c] = ZPIX ? zpi[q] : zs[c * A + ci[q]];
                 aw[q][c] = av[q][c] = avc[q][c] = 0.f;
             }
-        // halo row of pixel q at offset dy is (tr*kRows + q + R + dy); walk rows r relative to pixel 0.
         for (int r = -R; r <= R + kRows - 1; r++) {
             const int row = (tr * kRows + R + r) * hw + lx + R;
             float spq[kRows];
@@ -273,27 +283,25 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P)
 #pragma unroll 4
             for (int dx = -R; dx <= R; dx++) {
                 const int h = row + dx;
-                const float pen = vpen[h];
-                float fj[MF > 0 ? MF : 1];
-#pragma unroll
-                for (int f = 0; f < MF; f++) fj[f] = f < nf ? feat[(size_t)f * A + h] : 0.f;
+                const float dxs = fmaf(P.ds2, (float)(dx * dx), vpen[h]);
                 float lj[3], zj[3], vj[3], vcj[3];
+                const float zpj = ZPIX ? zpix[h] : 0.f;
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     lj[c] = ln[c * A + h];
-                    zj[c] = zs[c * A + h];
+                    zj[c] = ZPIX ? zpj : zs[c * A + h];
                     vj[c] = sv[c * A + h];
                     vcj[c] = LEVC ? svc[c * A + h] : 0.f;
                 }
-                const float dxs = fmaf(P.ds2, (float)(dx * dx), pen);
 #pragma unroll
                 for (int q = 0; q < kRows; q++) {
                     if (!use[q]) continue;
-                    const float w = exp2f(range_arg2<MF>(fi[q], fj, nf, spq[q] + dxs));
+                    const float w = fast_exp2(range_arg2<MF>(fi[q], feat, A, h, nf, spq[q] + dxs));
+                    const float zz = zi[q][0] + zj[0];
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         const float dl = li[q][c] - lj[c];
-                        const float t = fmaf(-dl, dl, zi[q][c] + zj[c]);
+                        const float t = fmaf(-dl, dl, ZPIX ? zz : zi[q][c] + zj[c]);
                         const float m = t >= 0.f ? w : 0.f;
                         aw[q][c] += m;
                         av[q][c] = fmaf(m, vj[c], av[q][c]);
@@ -365,7 +373,8 @@ __device__ __noinline__ int welch_exact(float diff, float di, float dj, int ni, 
 }
 
 // Mask layout: per pixel, per window row, ceil((2R+1)/32) words: bit dx+R of
-// row dy+R is set while the neighbour is still accepted.
+// row dy+R is set while the neighbour is still accepted. Rows are handled as
+// one 64-bit register value (2R+1 <= 41 bits).
 template <int MF, int kRows, int kThreadRows>
 __global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P) {
     constexpr int kTY = kRows * kThreadRows;
@@ -376,9 +385,9 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P)
     const int nf = P.feat.nch;
     const int t = threadIdx.x;
     uint32_t *mask = (uint32_t *)smem;                          // [kRows][D][wpr][kThreads]
-    int *nval = (int *)(mask + (size_t)kRows * D * wpr * kThreads);  // [A]
+    int *nval = (int *)(mask + kRows * D * wpr * kThreads);     // [A]
     float *feat = (float *)(nval + A);                          // [nf][A]
-    float *mu = feat + (size_t)nf * A;                          // [3][A] (film in the last pass)
+    float *mu = feat + nf * A;                                  // [3][A] (film in the last pass)
     float *dd = mu + 3 * A;                                     // [3][A]
     __shared__ int s_nmin, s_nmax;
 
@@ -386,8 +395,15 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P)
     const int lx = t % kTX2, tr = t / kTX2;
     const int x = x0 + lx;
     const size_t HW = (size_t)P.W * P.H;
-    auto MASK = [&](int q, int row, int w) -> uint32_t & {
-        return mask[(((size_t)q * D + row) * wpr + w) * kThreads + t];
+    auto mask_at = [&](int q, int row, int w) -> uint32_t & { return mask[((q * D + row) * wpr + w) * kThreads + t]; };
+    auto load_row = [&](int q, int row) -> uint64_t {
+        uint64_t v = mask_at(q, row, 0);
+        if (wpr > 1) v |= (uint64_t)mask_at(q, row, 1) << 32;
+        return v;
+    };
+    auto and_row = [&](int q, int row, uint64_t v) {
+        mask_at(q, row, 0) &= (uint32_t)v;
+        if (wpr > 1) mask_at(q, row, 1) &= (uint32_t)(v >> 32);
     };
 
     if (t == 0) {
@@ -396,7 +412,7 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P)
     }
     for (int q = 0; q < kRows; q++)
         for (int row = 0; row < D; row++)
-            for (int w = 0; w < wpr; w++) MASK(q, row, w) = 0xFFFFFFFFu;
+            for (int w = 0; w < wpr; w++) mask_at(q, row, w) = 0xFFFFFFFFu;
     __syncthreads();
     {
         int lmin = 0x7fffffff, lmax = 0;
@@ -418,7 +434,7 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P)
         atomicMax(&s_nmax, lmax);
     }
     for (int f = 0; f < nf; f++)
-        load_feat_scaled(feat + (size_t)f * A, P.feat.plane[f], P.feat.mul[f], P.W, P.H, x0, y0, R, hw, hh);
+        load_feat_scaled(feat + f * A, P.feat.plane[f], P.feat.mul[f], P.W, P.H, x0, y0, R, hw, hh);
     __syncthreads();
     // All valid n in the halo equal: the df bounds are the same for every pair.
     const bool uni = s_nmin == s_nmax;
@@ -475,28 +491,25 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P)
             if (P.bits && in[q])
                 for (int w = 0; w < fwords; w++) P.bits[(gi[q] * P.K + k) * (size_t)fwords + w] = 0u;
         }
-        // Only the transforms that feed the mask may skip already rejected pairs.
+        // Only transforms that feed the mask may skip pairs an earlier transform rejected.
         const bool skip_rejected = (P.bits == nullptr) && P.mt_mode == STATER_MT_ALL && k > 0;
         for (int r = -R; r <= R + kRows - 1; r++) {
             const int row = (tr * kRows + R + r) * hw + lx + R;
             bool use[kRows];
-            uint32_t prev[kRows][2], cur[kRows][2];
+            uint64_t prev[kRows], cur[kRows];
 #pragma unroll
             for (int q = 0; q < kRows; q++) {
                 const int dy = r - q;
                 use[q] = act[q] && dy >= -R && dy <= R;
-                cur[q][0] = cur[q][1] = 0u;
-                prev[q][0] = prev[q][1] = 0xFFFFFFFFu;
-                if (use[q] && skip_rejected) {
-                    prev[q][0] = MASK(q, dy + R, 0);
-                    if (wpr > 1) prev[q][1] = MASK(q, dy + R, 1);
-                }
+                cur[q] = 0ull;
+                prev[q] = ~0ull;
+                if (use[q] && skip_rejected) prev[q] = load_row(q, dy + R);
             }
 #pragma unroll 2
             for (int dx = -R; dx <= R; dx++) {
                 const int h = row + dx;
                 const int nj = nval[h];
-                const int b = dx + R, bw = b >> 5, bb = b & 31;
+                const int b = dx + R;
                 float mj[3], dj[3];
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
@@ -514,45 +527,43 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P)
                         tlo = dfl > kDfMax ? P.z2lo : __ldg(P.tlo + dfl);
                         thi = __ldg(P.thi + (dfh > kDfMax ? kDfMax : dfh));
                     }
+                    // qq <= tlo s accepts, qq > thi s rejects, in between the exact
+                    // df decides; s = 0 accepts exactly when the means are equal.
                     bool acc = true, amb = false;
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         const float diff = mi[q][c] - mj[c];
                         const float s = di[q][c] + dj[c];
                         const float qq = diff * diff;
-                        const bool pos = s > 0.f;
                         const bool lo = qq <= tlo * s;
-                        const bool hi = qq > thi * s;
-                        acc = acc && (pos ? !hi : diff == 0.f);
-                        amb = amb || (pos && !lo && !hi);
+                        const bool hi = qq <= thi * s;
+                        acc = acc && hi;
+                        amb = amb || (hi && !lo);
                     }
-                    int a = (acc && nj >= 2 && ((prev[q][bw] >> bb) & 1u)) ? 1 : 0;
+                    bool a = acc && nj >= 2 && ((prev[q] >> b) & 1ull);
                     if (a && amb) {
 #pragma unroll
                         for (int c = 0; c < 3; c++) {
                             const float diff = mi[q][c] - mj[c];
                             const float s = di[q][c] + dj[c];
                             const float qq = diff * diff;
-                            if (s > 0.f && !(qq <= tlo * s) && !(qq > thi * s))
-                                a &= welch_exact(diff, di[q][c], dj[c], ni[q], nj, P.lut, P.lut_n);
+                            if (!(qq <= tlo * s) && qq <= thi * s)
+                                a = a && welch_exact(diff, di[q][c], dj[c], ni[q], nj, P.lut, P.lut_n);
                         }
                     }
-                    if (dx == 0 && r == q) a = 1;
-                    cur[q][bw] |= (uint32_t)a << bb;
+                    if (dx == 0 && r == q) a = true;
+                    cur[q] |= (uint64_t)a << b;
                 }
             }
 #pragma unroll
             for (int q = 0; q < kRows; q++) {
                 if (!use[q]) continue;
                 const int dy = r - q;
-                if (andm[q]) {
-                    MASK(q, dy + R, 0) &= cur[q][0];
-                    if (wpr > 1) MASK(q, dy + R, 1) &= cur[q][1];
-                }
+                if (andm[q]) and_row(q, dy + R, cur[q]);
                 if (P.bits) {
                     uint32_t *fb = P.bits + (gi[q] * P.K + k) * (size_t)fwords;
                     for (int b = 0; b < D; b++) {
-                        if ((cur[q][b >> 5] >> (b & 31)) & 1u) {
+                        if ((cur[q] >> b) & 1ull) {
                             const int fbit = (dy + R) * D + b;
                             fb[fbit >> 5] |= 1u << (fbit & 31);
                         }
@@ -569,7 +580,7 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P)
 #pragma unroll
     for (int q = 0; q < kRows; q++)
 #pragma unroll
-        for (int f = 0; f < MF; f++) fi[q][f] = f < nf ? feat[(size_t)f * A + ci[q]] : 0.f;
+        for (int f = 0; f < MF; f++) fi[q][f] = f < nf ? feat[f * A + ci[q]] : 0.f;
 #pragma unroll
     for (int q = 0; q < kRows; q++) {
         if (!in[q]) continue;
@@ -581,18 +592,12 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P)
         for (int dy = -R; dy <= R; dy++) {
             const int row = (tr * kRows + q + R + dy) * hw + lx + R;
             const float sdy = P.ds2 * (float)(dy * dy);
-            const uint32_t m0 = MASK(q, dy + R, 0);
-            const uint32_t m1 = wpr > 1 ? MASK(q, dy + R, 1) : 0u;
+            const uint64_t m = load_row(q, dy + R);
 #pragma unroll 4
             for (int dx = -R; dx <= R; dx++) {
-                const int b = dx + R;
-                const uint32_t bit = ((b < 32 ? m0 : m1) >> (b & 31)) & 1u;
                 const int h = row + dx;
-                float fj[MF > 0 ? MF : 1];
-#pragma unroll
-                for (int f = 0; f < MF; f++) fj[f] = f < nf ? feat[(size_t)f * A + h] : 0.f;
-                const float e = range_arg2<MF>(fi[q], fj, nf, fmaf(P.ds2, (float)(dx * dx), sdy));
-                const float wt = bit ? exp2f(e) : 0.f;
+                const float e = range_arg2<MF>(fi[q], feat, A, h, nf, fmaf(P.ds2, (float)(dx * dx), sdy));
+                const float wt = ((m >> (dx + R)) & 1ull) ? fast_exp2(e) : 0.f;
                 sw += wt;
 #pragma unroll
                 for (int c = 0; c < 3; c++) sf[c] = fmaf(wt, mu[c * A + h], sf[c]);
@@ -652,9 +657,9 @@ const DfTables *df_tables(double alpha, cudaStream_t s) {
     return &t;
 }
 
-size_t vars_smem(int R, int nf, bool levc, int RB, int TR) {
+size_t vars_smem(int R, int nf, bool levc, bool zpix, int RB, int TR) {
     const size_t A = (size_t)(kTX2 + 2 * R) * (RB * TR + 2 * R);
-    return A * sizeof(float) * (1 + nf + 9 + (levc ? 3 : 0));
+    return A * sizeof(float) * (1 + nf + 6 + (zpix ? 1 : 3) + (levc ? 3 : 0));
 }
 
 size_t film_smem(int R, int nf, int RB, int TR) {
@@ -715,29 +720,32 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
     vars_stats_f32<<<g1, 128, 0, s>>>(P);
     STATER_CHECK_LAUNCH("vars_stats_f32");
 
+    const bool zp = P.max_moment < 4;
     int cfg = 0;
-    while (cfg < 3 && vars_smem(P.R, P.feat.nch, P.levc != 0, kTileCfg[cfg][0], kTileCfg[cfg][1]) > kSmemLimit) cfg++;
+    while (cfg < 3 && vars_smem(P.R, P.feat.nch, P.levc != 0, zp, kTileCfg[cfg][0], kTileCfg[cfg][1]) > kSmemLimit) cfg++;
     if (cfg == 3) return set_error(STATER_ERR_UNSUPPORTED, "stater_denoise_vars: radius too large for FP32 tiles");
     const int RB = kTileCfg[cfg][0], TR = kTileCfg[cfg][1];
-    const size_t sm = vars_smem(P.R, P.feat.nch, P.levc != 0, RB, TR);
+    const size_t sm = vars_smem(P.R, P.feat.nch, P.levc != 0, zp, RB, TR);
     dim3 grid((P.W + kTX2 - 1) / kTX2, (P.H + RB * TR - 1) / (RB * TR));
     const int mf = mf_bucket(P.feat.nch);
     cudaError_t e = cudaSuccess;
-#define STATER_VARS_LAUNCH(LV, MFV, RBV, TRV)                                                   \
-    if ((P.levc != 0) == LV && mf == MFV && RB == RBV && TR == TRV) {                           \
-        e = set_smem(vars_filter_f32<LV, MFV, RBV, TRV>, sm);                                   \
-        if (e == cudaSuccess) vars_filter_f32<LV, MFV, RBV, TRV><<<grid, kTX2 * TRV, sm, s>>>(P); \
+#define STATER_VARS_LAUNCH(LV, ZV, MFV, RBV, TRV)                                                      \
+    if ((P.levc != 0) == LV && zp == ZV && mf == MFV && RB == RBV && TR == TRV) {                      \
+        e = set_smem(vars_filter_f32<LV, ZV, MFV, RBV, TRV>, sm);                                      \
+        if (e == cudaSuccess) vars_filter_f32<LV, ZV, MFV, RBV, TRV><<<grid, kTX2 * TRV, sm, s>>>(P);  \
     }
-#define STATER_VARS_LAUNCH_T(RBV, TRV)                                                              \
-    STATER_VARS_LAUNCH(true, 0, RBV, TRV) STATER_VARS_LAUNCH(true, 4, RBV, TRV)                     \
-    STATER_VARS_LAUNCH(true, 8, RBV, TRV) STATER_VARS_LAUNCH(true, 16, RBV, TRV)                    \
-    STATER_VARS_LAUNCH(true, 24, RBV, TRV) STATER_VARS_LAUNCH(false, 0, RBV, TRV)                   \
-    STATER_VARS_LAUNCH(false, 4, RBV, TRV) STATER_VARS_LAUNCH(false, 8, RBV, TRV)                   \
-    STATER_VARS_LAUNCH(false, 16, RBV, TRV) STATER_VARS_LAUNCH(false, 24, RBV, TRV)
+#define STATER_VARS_LAUNCH_M(LV, ZV, RBV, TRV)                                                          \
+    STATER_VARS_LAUNCH(LV, ZV, 0, RBV, TRV) STATER_VARS_LAUNCH(LV, ZV, 4, RBV, TRV)                      \
+    STATER_VARS_LAUNCH(LV, ZV, 8, RBV, TRV) STATER_VARS_LAUNCH(LV, ZV, 16, RBV, TRV)                     \
+    STATER_VARS_LAUNCH(LV, ZV, 24, RBV, TRV)
+#define STATER_VARS_LAUNCH_T(RBV, TRV)                                                                  \
+    STATER_VARS_LAUNCH_M(true, false, RBV, TRV) STATER_VARS_LAUNCH_M(false, false, RBV, TRV)             \
+    STATER_VARS_LAUNCH_M(true, true, RBV, TRV) STATER_VARS_LAUNCH_M(false, true, RBV, TRV)
     STATER_VARS_LAUNCH_T(STATER_TILE_RB, STATER_TILE_TR)
     if (cfg == 1) { STATER_VARS_LAUNCH_T(1, 4) }
     if (cfg == 2) { STATER_VARS_LAUNCH_T(1, 2) }
 #undef STATER_VARS_LAUNCH_T
+#undef STATER_VARS_LAUNCH_M
 #undef STATER_VARS_LAUNCH
     if (e != cudaSuccess) return cuda_status(e, "vars_filter_f32 smem attribute");
     STATER_CHECK_LAUNCH("vars_filter_f32");
