@@ -18,9 +18,6 @@
 
 #include "common.cuh"
 
-#ifndef STATER_ACC_LOOKAHEAD
-#define STATER_ACC_LOOKAHEAD 1
-#endif
 
 namespace stater {
 
@@ -100,6 +97,63 @@ __device__ __forceinline__ T acc_transform(float lambda, T x) {
     }
 }
 
+// One sample's update of one transform's moments (3 channels). `cur` holds
+// R, G, B and, with MAXMOM >= 5, the in-pixel offsets u, v.
+template <typename T, bool FAST, int MAXMOM, int KIND>
+__device__ __forceinline__ void acc_update(const float *cur, uint32_t nn, float lam, T (&mean)[3], T (&m2)[3],
+                                           T (&m3)[3], T (&m4)[3], T (&cx)[3], T (&cy)[3], T (&m1)[3], T &rn_out) {
+    const T nT = (T)nn;
+    T rn = T(0);
+    if (FAST) rn = T(1) / nT;
+    rn_out = rn;
+    float xD = 0.f, yD = 0.f;
+    if (MAXMOM >= 5) {
+        xD = cur[3] - 0.5f;
+        yD = cur[4] - 0.5f;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const T x = acc_transform<T, FAST, KIND>(lam, (T)cur[c]);
+        if (FAST && nn == 1u) {
+            // First sample: the update reduces to mean = x with every central
+            // moment exactly 0. Taking that directly keeps FMA contraction from
+            // leaving rounding residue of the size of x^3 in m3 (the EXACT form
+            // computes the reference's update, which gives 0 here as well).
+            mean[c] = x;
+            continue;
+        }
+        const T d = x - mean[c];
+        const T dN = FAST ? d * rn : d / nT;
+        if (MAXMOM <= 1) {
+            mean[c] = mean[c] + dN;
+        } else if (MAXMOM == 2) {
+            mean[c] = mean[c] + dN;
+            m2[c] = m2[c] + d * (d - dN);
+        } else {
+            const T d2 = d * d;
+            const T dN2 = dN * dN;
+            mean[c] = mean[c] + dN;
+            m2[c] = m2[c] + d * (d - dN);
+            m3[c] = m3[c] + ((T)-3.f * dN * m2[c] + d * (d2 - dN2));
+            if (MAXMOM >= 4)
+                m4[c] = m4[c] + (((T)-4.f * dN * m3[c] - (T)6.f * dN2 * m2[c]) + d * (d * d2 - dN * dN2));
+            if (MAXMOM >= 5) {
+                cx[c] = cx[c] + (x - mean[c]) * (T)xD;
+                cy[c] = cy[c] + (x - mean[c]) * (T)yD;
+                m1[c] = m1[c] + sqrt(d * (d - dN));
+            }
+        }
+    }
+}
+
+// Running mean of a feature channel (AddSampleM1 of a G-buffer tile).
+template <typename T, bool FAST>
+__device__ __forceinline__ void feat_update(float v, uint32_t nn, T rn, T &fm) {
+    const T d = (T)v - fm;
+    const T dN = FAST ? d * rn : d / (T)nn;
+    fm = fm + dN;
+}
+
 template <typename T, bool FAST, int MAXMOM, int MAXF, int KIND>
 __device__ __forceinline__ void acc_loop(const AccParams &P, size_t p, int k, int cnt, uint32_t n0, float lam,
                                          T (&mean)[3], T (&m2)[3], T (&m3)[3], T (&m4)[3], T (&cx)[3],
@@ -108,73 +162,29 @@ __device__ __forceinline__ void acc_loop(const AccParams &P, size_t p, int k, in
     const float *sp = P.samples + p;
     const size_t sstride = (size_t)P.NCH * HW;
     constexpr int NL = MAXMOM >= 5 ? 5 : 3;
-    // A ring of LA samples stays in flight per thread: the slot just consumed is
-    // refilled with the sample LA steps ahead before the current one is processed.
-    constexpr int LA = STATER_ACC_LOOKAHEAD;
-    float ring[LA][NL];
+    // The next sample's loads are issued before the current one is processed.
+    float nxt[NL];
+    if (cnt > 0) {
 #pragma unroll
-    for (int j = 0; j < LA; j++)
-        if (j < cnt) {
-#pragma unroll
-            for (int c = 0; c < NL; c++) ring[j][c] = __ldg(sp + (size_t)j * sstride + (size_t)c * HW);
-        }
-    for (int s0 = 0; s0 < cnt; s0 += LA) {
-#pragma unroll
-    for (int j = 0; j < LA; j++) {
-        const int s = s0 + j;
-        if (s >= cnt) break;
+        for (int c = 0; c < NL; c++) nxt[c] = __ldg(sp + (size_t)c * HW);
+    }
+    for (int s = 0; s < cnt; s++) {
         float cur[NL];
 #pragma unroll
-        for (int c = 0; c < NL; c++) cur[c] = ring[j][c];
+        for (int c = 0; c < NL; c++) cur[c] = nxt[c];
         const float *spc = sp + (size_t)s * sstride;
-        if (s + LA < cnt) {
+        if (s + 1 < cnt) {
 #pragma unroll
-            for (int c = 0; c < NL; c++) ring[j][c] = __ldg(spc + (size_t)LA * sstride + (size_t)c * HW);
+            for (int c = 0; c < NL; c++) nxt[c] = __ldg(spc + sstride + (size_t)c * HW);
         }
         const uint32_t nn = n0 + (uint32_t)s + 1u;
-        const T nT = (T)nn;
-        T rn = T(0);
-        if (FAST) rn = T(1) / nT;
-        float xD = 0.f, yD = 0.f;
-        if (MAXMOM >= 5) {
-            xD = cur[3] - 0.5f;
-            yD = cur[4] - 0.5f;
-        }
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const T x = acc_transform<T, FAST, KIND>(lam, (T)cur[c]);
-            const T d = x - mean[c];
-            const T dN = FAST ? d * rn : d / nT;
-            if (MAXMOM <= 1) {
-                mean[c] = mean[c] + dN;
-            } else if (MAXMOM == 2) {
-                mean[c] = mean[c] + dN;
-                m2[c] = m2[c] + d * (d - dN);
-            } else {
-                const T d2 = d * d;
-                const T dN2 = dN * dN;
-                mean[c] = mean[c] + dN;
-                m2[c] = m2[c] + d * (d - dN);
-                m3[c] = m3[c] + ((T)-3.f * dN * m2[c] + d * (d2 - dN2));
-                if (MAXMOM >= 4)
-                    m4[c] = m4[c] + (((T)-4.f * dN * m3[c] - (T)6.f * dN2 * m2[c]) + d * (d * d2 - dN * dN2));
-                if (MAXMOM >= 5) {
-                    cx[c] = cx[c] + (x - mean[c]) * (T)xD;
-                    cy[c] = cy[c] + (x - mean[c]) * (T)yD;
-                    m1[c] = m1[c] + sqrt(d * (d - dN));
-                }
-            }
-        }
+        T rn;
+        acc_update<T, FAST, MAXMOM, KIND>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
 #pragma unroll
         for (int jf = 0; jf < MAXF; jf++) {
             const int g = k + jf * P.K;
-            if (g < P.G) {
-                const T d = (T)__ldg(spc + (size_t)(5 + g) * HW) - fm[jf];
-                const T dN = FAST ? d * rn : d / nT;
-                fm[jf] = fm[jf] + dN;
-            }
+            if (g < P.G) feat_update<T, FAST>(__ldg(spc + (size_t)(5 + g) * HW), nn, rn, fm[jf]);
         }
-    }
     }
 }
 
@@ -182,11 +192,15 @@ template <typename T, bool FAST, int MAXMOM, int MAXF>
 __global__ void __launch_bounds__(256) acc_kernel(AccParams P) {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int k = threadIdx.y;
-    if (p >= P.HW) return;
+    const bool valid = p < P.HW;
+    // Every transform's thread reads n before the transform-0 thread of the same
+    // pixel may write the updated count back.
+    const uint32_t n0 = valid ? (uint32_t)P.n[p] : 0u;
+    __syncthreads();
+    if (!valid) return;
     const size_t HW = P.HW;
     // per-pixel counts beyond the S sample planes are clamped (never read past them)
     const int cnt = P.count ? min(max(P.count[p], 0), P.S) : P.S;
-    const uint32_t n0 = (uint32_t)P.n[p];
     T *st = (T *)P.stats;
     T *gm = (T *)P.gmean;
 

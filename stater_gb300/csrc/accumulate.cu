@@ -9,6 +9,7 @@
 namespace stater {
 
 cudaError_t launch_acc_fast_f32(const AccParams &P, int max_moment, cudaStream_t s);
+cudaError_t launch_acc_tma_f32(const AccParams &P, int max_moment, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Synthetic sample source.
@@ -238,8 +239,13 @@ stater_status stater_accumulate(const stater_accumulate_args *a, stater_stream s
     P.gmean = a->gmean;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e;
-    if (a->mode == STATER_ACC_FAST)
-        e = launch_acc_fast_f32(P, a->max_moment, s);
+    if (a->mode == STATER_ACC_FAST) {
+        e = launch_acc_tma_f32(P, a->max_moment, s);
+        if (e == cudaErrorNotSupported) {
+            cudaGetLastError();
+            e = launch_acc_fast_f32(P, a->max_moment, s);
+        }
+    }
     else if (a->precision == STATER_F64)
         e = launch_acc<double, false>(P, a->max_moment, s);
     else

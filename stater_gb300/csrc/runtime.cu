@@ -1,5 +1,6 @@
 // Library runtime: error reporting, setup, per-device scratch and the cached
 // Student-t critical-value tables. Host code only.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -32,6 +33,12 @@ std::mutex g_mutex;
 std::map<std::tuple<int, cudaStream_t, int>, ScratchBuf> g_scratch;
 std::map<std::pair<int, double>, LutEntry> g_luts;
 std::map<int, int> g_sm_count;
+std::map<int, int *> g_err_word;
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn g_encode = nullptr;
 
 constexpr int kLutIntervals = 1024;
 }  // namespace
@@ -90,6 +97,50 @@ void *scratch(int slot, size_t bytes, cudaStream_t stream) {
 
 int tcrit_intervals() { return kLutIntervals; }
 
+// One int per device that kernels set when a bounded wait gives up.
+int *device_error_word() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_mutex);
+    int *&w = g_err_word[dev];
+    if (!w) {
+        if (cudaMalloc(&w, sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            w = nullptr;
+            return nullptr;
+        }
+        cudaMemset(w, 0, sizeof(int));
+    }
+    return w;
+}
+
+// 2-D fp32 tensor map over a row-major [rows][cols] array (cols contiguous),
+// boxes of box_rows x box_cols, out-of-range elements read as zero.
+bool encode_tensor_map_2d_f32(CUtensorMap *map, const void *base, uint64_t cols, uint64_t rows, uint32_t box_cols,
+                              uint32_t box_rows) {
+    {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        if (!g_encode) {
+            void *fn = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                    cudaSuccess ||
+                q != cudaDriverEntryPointSuccess || !fn) {
+                cudaGetLastError();
+                return false;
+            }
+            g_encode = (EncodeTiledFn)fn;
+        }
+    }
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * 4};
+    const cuuint32_t box[2] = {box_cols, box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 const void *tcrit_table_device(double alpha, bool f64, cudaStream_t stream) {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -139,7 +190,27 @@ stater_status stater_setup(void) {
 
 stater_status stater_synchronize(stater_stream stream) {
     clear_error();
-    return cuda_status(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
+    stater_status st = cuda_status(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
+    if (st != STATER_OK) return st;
+    int *w = nullptr;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        std::lock_guard<std::mutex> lk(g_mutex);
+        auto it = g_err_word.find(dev);
+        if (it != g_err_word.end()) w = it->second;
+    }
+    if (w) {
+        int v = 0;
+        cudaError_t e = cudaMemcpy(&v, w, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_status(e, "stater_synchronize: error word");
+        if (v != 0) {
+            cudaMemset(w, 0, sizeof(int));
+            return set_error(STATER_ERR_TIMEOUT, "a bounded device wait gave up (pipeline stalled); results of the "
+                                                 "affected call are incomplete");
+        }
+    }
+    return STATER_OK;
 }
 
 void stater_print_macro_configuration(void) {
@@ -167,6 +238,13 @@ stater_status stater_release_cache(void) {
             it = g_scratch.erase(it);
         } else {
             ++it;
+        }
+    }
+    {
+        auto it = g_err_word.find(dev);
+        if (it != g_err_word.end()) {
+            cudaFree(it->second);
+            g_err_word.erase(it);
         }
     }
     for (auto it = g_luts.begin(); it != g_luts.end();) {
