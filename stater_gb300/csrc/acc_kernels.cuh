@@ -97,14 +97,48 @@ __device__ __forceinline__ T acc_transform(float lambda, T x) {
     }
 }
 
+// One sample's update of one transform's moments for one channel.
+template <typename T, bool FAST, int MAXMOM>
+__device__ __forceinline__ void acc_update1(T x, uint32_t nn, T rn, float xD, float yD, T &mean, T &m2, T &m3, T &m4,
+                                            T &cx, T &cy, T &m1) {
+    const T nT = (T)nn;
+    if (FAST && nn == 1u) {
+        // First sample: the update reduces to mean = x with every central
+        // moment exactly 0. Taking that directly keeps FMA contraction from
+        // leaving rounding residue of the size of x^3 in m3 (the EXACT form
+        // computes the reference's update, which gives 0 here as well).
+        mean = x;
+        return;
+    }
+    const T d = x - mean;
+    const T dN = FAST ? d * rn : d / nT;
+    if (MAXMOM <= 1) {
+        mean = mean + dN;
+    } else if (MAXMOM == 2) {
+        mean = mean + dN;
+        m2 = m2 + d * (d - dN);
+    } else {
+        const T d2 = d * d;
+        const T dN2 = dN * dN;
+        mean = mean + dN;
+        m2 = m2 + d * (d - dN);
+        m3 = m3 + ((T)-3.f * dN * m2 + d * (d2 - dN2));
+        if (MAXMOM >= 4) m4 = m4 + (((T)-4.f * dN * m3 - (T)6.f * dN2 * m2) + d * (d * d2 - dN * dN2));
+        if (MAXMOM >= 5) {
+            cx = cx + (x - mean) * (T)xD;
+            cy = cy + (x - mean) * (T)yD;
+            m1 = m1 + sqrt(d * (d - dN));
+        }
+    }
+}
+
 // One sample's update of one transform's moments (3 channels). `cur` holds
 // R, G, B and, with MAXMOM >= 5, the in-pixel offsets u, v.
 template <typename T, bool FAST, int MAXMOM, int KIND>
 __device__ __forceinline__ void acc_update(const float *cur, uint32_t nn, float lam, T (&mean)[3], T (&m2)[3],
                                            T (&m3)[3], T (&m4)[3], T (&cx)[3], T (&cy)[3], T (&m1)[3], T &rn_out) {
-    const T nT = (T)nn;
     T rn = T(0);
-    if (FAST) rn = T(1) / nT;
+    if (FAST) rn = T(1) / (T)nn;
     rn_out = rn;
     float xD = 0.f, yD = 0.f;
     if (MAXMOM >= 5) {
@@ -114,35 +148,19 @@ __device__ __forceinline__ void acc_update(const float *cur, uint32_t nn, float 
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         const T x = acc_transform<T, FAST, KIND>(lam, (T)cur[c]);
-        if (FAST && nn == 1u) {
-            // First sample: the update reduces to mean = x with every central
-            // moment exactly 0. Taking that directly keeps FMA contraction from
-            // leaving rounding residue of the size of x^3 in m3 (the EXACT form
-            // computes the reference's update, which gives 0 here as well).
-            mean[c] = x;
-            continue;
-        }
-        const T d = x - mean[c];
-        const T dN = FAST ? d * rn : d / nT;
-        if (MAXMOM <= 1) {
-            mean[c] = mean[c] + dN;
-        } else if (MAXMOM == 2) {
-            mean[c] = mean[c] + dN;
-            m2[c] = m2[c] + d * (d - dN);
-        } else {
-            const T d2 = d * d;
-            const T dN2 = dN * dN;
-            mean[c] = mean[c] + dN;
-            m2[c] = m2[c] + d * (d - dN);
-            m3[c] = m3[c] + ((T)-3.f * dN * m2[c] + d * (d2 - dN2));
-            if (MAXMOM >= 4)
-                m4[c] = m4[c] + (((T)-4.f * dN * m3[c] - (T)6.f * dN2 * m2[c]) + d * (d * d2 - dN * dN2));
-            if (MAXMOM >= 5) {
-                cx[c] = cx[c] + (x - mean[c]) * (T)xD;
-                cy[c] = cy[c] + (x - mean[c]) * (T)yD;
-                m1[c] = m1[c] + sqrt(d * (d - dN));
-            }
-        }
+        acc_update1<T, FAST, MAXMOM>(x, nn, rn, xD, yD, mean[c], m2[c], m3[c], m4[c], cx[c], cy[c], m1[c]);
+    }
+}
+
+// FAST transform chosen at run time (the kind is uniform across a warp).
+__device__ __forceinline__ float fast_transform_rt(int kind, float lam, float x) {
+    switch (kind) {
+        case STATER_TK_LOG1P: return acc_transform<float, true, STATER_TK_LOG1P>(lam, x);
+        case STATER_TK_SQRT: return acc_transform<float, true, STATER_TK_SQRT>(lam, x);
+        case STATER_TK_CBRT: return acc_transform<float, true, STATER_TK_CBRT>(lam, x);
+        case STATER_TK_ASINH: return acc_transform<float, true, STATER_TK_ASINH>(lam, x);
+        case STATER_TK_BOXCOX: return acc_transform<float, true, STATER_TK_BOXCOX>(lam, x);
+        default: return x;
     }
 }
 
