@@ -297,6 +297,64 @@ stater_status stater_lev_solve(int32_t width, int32_t height, int32_t n_features
                                stater_precision precision, const void *state, double lambda,
                                void *beta, void *m2C, void *r2, stater_stream stream);
 
+/* ---- serving: continuous batching of denoise jobs ---------------------- */
+
+/* A server owns `max_slots` CUDA streams on the current device and one
+ * scheduler thread. Jobs are admitted in arrival order as soon as a slot is free
+ * and their device-memory footprint fits under `hbm_budget_bytes` together with
+ * the jobs already running, so jobs that arrive while others are on the GPU start
+ * without waiting for them and their work overlaps on the device. Each job
+ * generates its samples on the device (the seeded synthetic source), accumulates
+ * them, runs denoiseVars and denoiseFilm, and copies the denoised film to
+ * `out_host`. With rounds > 1 a job is rendered adaptively: after each round its
+ * moment buffers stay on the device, calcTargetSPP allots the next round's
+ * samples (spp on average per pixel, clamped to [16, 1024]) and the round's
+ * samples continue every pixel's own sample sequence. Results are independent of
+ * what else runs: a job gives the same output alone and in any mix. */
+typedef struct stater_server stater_server;
+
+typedef struct {
+    int32_t max_slots;          /* concurrent jobs (streams), 1..64 */
+    double hbm_budget_bytes;    /* admission limit; <= 0: 80% of the free memory at creation */
+    int32_t precision;          /* STATER_F32 (serving form) or STATER_F64 (plain form) */
+    int32_t chunk_spp;          /* samples generated and accumulated per step (default 32) */
+} stater_server_config;
+
+typedef struct {
+    int32_t width, height;
+    int32_t spp;                /* samples per pixel (first round, and average per later round) */
+    int32_t rounds;             /* 1 = one pass */
+    int32_t n_transforms;
+    stater_transform transforms[STATER_MAX_TRANSFORMS];
+    int32_t n_features;         /* feature channels generated; the range kernels use albedo (0-2, sigma 0.02),
+                                   normal (3-5, 0.1) and depth (6, 0.1) when present */
+    int32_t max_moment;         /* 3..5 */
+    int32_t filter_radius;
+    float filter_sd, alpha, var_z;
+    uint64_t seed;
+    float *out_host;            /* [3][H][W] float32, written when the job completes (may be NULL) */
+} stater_job_desc;
+
+typedef enum { STATER_JOB_QUEUED = 0, STATER_JOB_RUNNING = 1, STATER_JOB_DONE = 2, STATER_JOB_FAILED = 3 } stater_job_state;
+
+typedef struct {
+    int64_t submitted, completed, failed, running, queued;
+    double latency_p50_ms, latency_p99_ms, latency_mean_ms;
+    double mpix_per_s;          /* pixels of completed jobs / (last completion - first submission) */
+    double peak_footprint_bytes;
+} stater_server_stats;
+
+stater_status stater_server_create(const stater_server_config *cfg, stater_server **out);
+stater_status stater_server_submit(stater_server *srv, const stater_job_desc *job, int64_t *job_id);
+stater_status stater_server_poll(stater_server *srv, int64_t job_id, int32_t *state, double *latency_ms);
+/* Blocks until the job is done or failed, or timeout_s elapses (STATER_ERR_TIMEOUT). */
+stater_status stater_server_wait(stater_server *srv, int64_t job_id, double timeout_s);
+stater_status stater_server_drain(stater_server *srv, double timeout_s);
+stater_status stater_server_stats_get(stater_server *srv, stater_server_stats *out);
+/* Device bytes a job needs while it runs (the admission footprint). */
+double stater_job_footprint(const stater_job_desc *job, int32_t precision, int32_t chunk_spp);
+stater_status stater_server_destroy(stater_server *srv);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,574 @@
+// Serving engine: continuous admission of denoise jobs onto stream slots.
+//
+// One scheduler thread owns the device work of all jobs. Each admitted job gets
+// a slot (a non-blocking CUDA stream) and one stream-ordered allocation
+// (cudaMallocAsync from the device's memory pool) holding its sample chunk,
+// moment buffers and outputs. A job is a small state machine: its rounds are
+// enqueued on its stream, and a CUDA event marks the point where the scheduler
+// must look again (the next round needs the largest per-pixel sample target of
+// the previous one; the last round ends with the device-to-host copy of the
+// denoised film). Between events the scheduler only polls, so work of all slots
+// runs concurrently on the device and new jobs are admitted the moment a slot
+// and enough memory are free.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "common.cuh"
+
+namespace stater {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+constexpr int kTmin = 16, kTmax = 1024;
+constexpr double kEps = 1e-4;
+
+__global__ void chunk_counts_kernel(size_t HW, const int32_t *target, int done, int chunk, int32_t *counts) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= HW) return;
+    counts[p] = max(0, min(target[p] - done, chunk));
+}
+
+__global__ void max_kernel(size_t HW, const int32_t *v, int32_t *out) {
+    int m = 0;
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < HW; p += (size_t)gridDim.x * blockDim.x)
+        m = max(m, v[p]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct Layout {
+    size_t HW, T, K, G, chunk;
+    size_t off_n, off_counts, off_target, off_max, off_stats, off_gmean, off_jb, off_out6, off_filmD, off_samples, total;
+};
+
+int chunk_for(const stater_job_desc &d, int chunk_spp) {
+    const size_t HW = (size_t)d.width * d.height;
+    const size_t per = (size_t)(5 + d.n_features) * HW * 4;
+    int c = std::max(1, chunk_spp > 0 ? chunk_spp : 32);
+    while (c > 1 && (size_t)c * per > ((size_t)2 << 30)) c /= 2;  // at most 2 GiB of sample planes per step
+    return c;
+}
+
+Layout layout(const stater_job_desc &d, int precision, int chunk_spp) {
+    Layout L;
+    L.HW = (size_t)d.width * d.height;
+    L.T = precision == STATER_F64 ? 8 : 4;
+    L.K = d.n_transforms;
+    L.G = d.n_features;
+    L.chunk = chunk_for(d, chunk_spp);
+    size_t o = 0;
+    auto take = [&](size_t b) {
+        const size_t r = o;
+        o += align256(b);
+        return r;
+    };
+    L.off_n = take(4 * L.HW);
+    L.off_counts = take(4 * L.HW);
+    L.off_target = take(4 * L.HW);
+    L.off_max = take(4);
+    L.off_stats = take(L.K * STATER_NQ * 3 * L.HW * L.T);
+    L.off_gmean = take(std::max<size_t>(L.G, 1) * L.HW * L.T);
+    L.off_jb = take(L.K * L.HW * L.T);
+    L.off_out6 = take(6 * L.K * 3 * L.HW * L.T);
+    L.off_filmD = take(3 * L.HW * L.T);
+    L.off_samples = take(L.chunk * (5 + L.G) * L.HW * 4);
+    L.total = o;
+    return L;
+}
+
+// Scratch the library's denoise and target-SPP calls keep per stream.
+size_t scratch_bytes(const Layout &L) {
+    const size_t vars = 2 * 3 * L.K * L.HW * L.T;
+    const size_t film = L.T == 8 ? 3 * L.K * L.HW * 8 : 0;
+    const size_t tspp = 8 * (L.HW + 2 * ((L.HW + 1023) / 1024) + 2);
+    return vars + film + tspp;
+}
+
+struct Job {
+    int64_t id = 0;
+    stater_job_desc d{};
+    Layout L{};
+    int state = STATER_JOB_QUEUED;
+    int slot = -1;
+    int round = 0;
+    bool final_enqueued = false;
+    double footprint = 0;
+    unsigned char *base = nullptr;
+    cudaEvent_t ev = nullptr;
+    Clock::time_point t_submit, t_done;
+    double latency_ms = 0;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    int32_t *hmax = nullptr;  // pinned: largest target of the last round
+    bool busy = false;
+};
+
+}  // namespace
+}  // namespace stater
+
+using namespace stater;
+
+struct stater_server {
+    stater_server_config cfg{};
+    int device = 0;
+    double budget = 0, used = 0, peak = 0;
+    std::vector<Slot> slots;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<Job>> queue;
+    std::vector<std::shared_ptr<Job>> active;
+    std::map<int64_t, std::shared_ptr<Job>> jobs;
+    int64_t next_id = 1;
+    bool stop = false;
+    std::thread worker;
+    std::vector<double> latencies;
+    int64_t submitted = 0, completed = 0, failed = 0;
+    double pixels_done = 0;
+    bool have_first = false;
+    Clock::time_point first_submit, last_done;
+
+    void run();
+    bool start(Job &j);
+    bool enqueue_round(Job &j, int samples, bool uniform);
+    bool enqueue_after_round(Job &j);
+    void finish(Job &j, bool ok);
+};
+
+namespace {
+
+stater_precision prec_of(const stater_server *s) { return (stater_precision)s->cfg.precision; }
+
+void fill_gbuffers(stater_gbuffers &g, const Job &j) {
+    std::memset(&g, 0, sizeof(g));
+    const int G = j.d.n_features;
+    const size_t plane = j.L.HW * j.L.T;
+    unsigned char *gm = j.base + j.L.off_gmean;
+    const float sig[3] = {0.02f, 0.1f, 0.1f};
+    const int first[3] = {0, 3, 6}, chans[3] = {3, 3, 1};
+    for (int i = 0; i < 3; i++) {
+        if (first[i] + chans[i] > G) break;
+        g.planes[g.count] = gm + first[i] * plane;
+        g.channels[g.count] = chans[i];
+        g.dr_factor[g.count] = -0.5f / (sig[i] * sig[i]);
+        g.count++;
+    }
+}
+
+}  // namespace
+
+bool stater_server::enqueue_round(Job &j, int samples, bool uniform) {
+    const Slot &sl = slots[j.slot];
+    cudaStream_t s = sl.stream;
+    const Layout &L = j.L;
+    int32_t *n = (int32_t *)(j.base + L.off_n);
+    int32_t *counts = (int32_t *)(j.base + L.off_counts);
+    int32_t *target = (int32_t *)(j.base + L.off_target);
+    float *smp = (float *)(j.base + L.off_samples);
+    for (int done = 0; done < samples; done += (int)L.chunk) {
+        const int S = std::min((int)L.chunk, samples - done);
+        if (!uniform) {
+            chunk_counts_kernel<<<(unsigned)((L.HW + 255) / 256), 256, 0, s>>>(L.HW, target, done, S, counts);
+            if (cudaGetLastError() != cudaSuccess) return false;
+        }
+        stater_generate_args g{};
+        g.width = j.d.width;
+        g.height = j.d.height;
+        g.n_samples = S;
+        g.n_features = j.d.n_features;
+        g.seed = j.d.seed;
+        g.region = 8;
+        g.mean_mu = -1.f;
+        g.mean_sigma = 1.f;
+        g.noise_sigma = 0.5f;
+        g.firefly_prob = 1e-3f;
+        g.firefly_scale = 1e3f;
+        g.first_index = n;  // every pixel continues its own sample sequence
+        g.samples = smp;
+        if (stater_generate_samples(&g, (stater_stream)s) != STATER_OK) return false;
+        stater_accumulate_args a{};
+        a.width = j.d.width;
+        a.height = j.d.height;
+        a.n_samples = S;
+        a.n_features = j.d.n_features;
+        a.samples = smp;
+        a.count = uniform ? nullptr : counts;
+        a.n_transforms = j.d.n_transforms;
+        for (int k = 0; k < j.d.n_transforms; k++) a.transforms[k] = j.d.transforms[k];
+        a.max_moment = j.d.max_moment;
+        a.precision = prec_of(this);
+        a.mode = prec_of(this) == STATER_F32 ? STATER_ACC_FAST : STATER_ACC_EXACT;
+        a.n = n;
+        a.stats = j.base + L.off_stats;
+        a.gmean = j.base + L.off_gmean;
+        if (stater_accumulate(&a, (stater_stream)s) != STATER_OK) return false;
+    }
+    return true;
+}
+
+// After a round: denoise the variance; then either allot the next round's
+// samples (and fetch their maximum) or filter the film and copy it out.
+bool stater_server::enqueue_after_round(Job &j) {
+    const Slot &sl = slots[j.slot];
+    cudaStream_t s = sl.stream;
+    const Layout &L = j.L;
+    const size_t plane3 = 3 * L.HW * L.T;
+    unsigned char *out6 = j.base + L.off_out6;
+    auto out_of = [&](int which, int k) { return (void *)(out6 + ((size_t)which * L.K + k) * plane3); };
+    unsigned char *stats = j.base + L.off_stats;
+    auto moment = [&](int k, int q) { return (void *)(stats + ((size_t)k * STATER_NQ + q) * plane3); };
+    stater_gbuffers gb;
+    fill_gbuffers(gb, j);
+    stater_denoise_vars_args v{};
+    v.n_buffers = j.d.n_transforms;
+    v.width = j.d.width;
+    v.height = j.d.height;
+    v.filter_radius = j.d.filter_radius;
+    v.ds_factor = -0.5f / (j.d.filter_sd * j.d.filter_sd);
+    v.var_z = j.d.var_z;
+    v.max_moment = j.d.max_moment;
+    v.precision = prec_of(this);
+    v.n = (const int32_t *)(j.base + L.off_n);
+    for (int k = 0; k < j.d.n_transforms; k++) {
+        v.m2[k] = moment(k, STATER_Q_M2);
+        v.m3[k] = moment(k, STATER_Q_M3);
+        v.m4[k] = moment(k, STATER_Q_M4);
+        v.c2X[k] = moment(k, STATER_Q_C2X);
+        v.c2Y[k] = moment(k, STATER_Q_C2Y);
+        v.jb[k] = j.base + L.off_jb + (size_t)k * L.HW * L.T;
+        v.lnS2[k] = out_of(0, k);
+        v.se2[k] = out_of(1, k);
+        v.m2C[k] = out_of(2, k);
+        v.varD[k] = out_of(3, k);
+        v.varCD[k] = out_of(4, k);
+    }
+    v.gbuffers = gb;
+    if (stater_denoise_vars(&v, (stater_stream)s) != STATER_OK) return false;
+    j.round++;
+    if (j.round < j.d.rounds) {
+        int32_t *target = (int32_t *)(j.base + L.off_target);
+        if (stater_calc_target_spp(j.d.width, j.d.height, j.d.spp, prec_of(this), v.n, v.varD[0], moment(0, STATER_Q_MEAN),
+                                   kEps, kTmin, kTmax, target, (stater_stream)s) != STATER_OK)
+            return false;
+        int32_t *dmax = (int32_t *)(j.base + L.off_max);
+        if (cudaMemsetAsync(dmax, 0, 4, s) != cudaSuccess) return false;
+        max_kernel<<<std::max(1, std::min(1024, (int)((L.HW + 255) / 256))), 256, 0, s>>>(L.HW, target, dmax);
+        if (cudaGetLastError() != cudaSuccess) return false;
+        if (cudaMemcpyAsync(sl.hmax, dmax, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return false;
+    } else {
+        stater_denoise_film_args f{};
+        f.n_buffers = j.d.n_transforms;
+        f.width = j.d.width;
+        f.height = j.d.height;
+        f.filter_radius = j.d.filter_radius;
+        f.ds_factor = v.ds_factor;
+        f.alpha = j.d.alpha;
+        f.mt_mode = STATER_MT_ALL;
+        f.use_levc = j.d.max_moment >= 5 ? 1 : 0;
+        f.precision = prec_of(this);
+        f.n = v.n;
+        f.film = moment(0, STATER_Q_MEAN);
+        for (int k = 0; k < j.d.n_transforms; k++) {
+            f.mean[k] = moment(k, STATER_Q_MEAN);
+            f.varD[k] = v.varD[k];
+            f.varCD[k] = v.varCD[k];
+            f.jb[k] = v.jb[k];
+            f.discr[k] = out_of(5, k);
+        }
+        f.gbuffers = gb;
+        f.filmD = j.base + L.off_filmD;
+        if (stater_denoise_film(&f, (stater_stream)s) != STATER_OK) return false;
+        if (j.d.out_host) {
+            if (L.T == 4) {
+                if (cudaMemcpyAsync(j.d.out_host, f.filmD, 3 * L.HW * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+                    return false;
+            } else {
+                // plain FP64 form: the film is delivered as float32 like the FP32 form
+                return false;
+            }
+        }
+        j.final_enqueued = true;
+    }
+    return cudaEventRecord(j.ev, s) == cudaSuccess;
+}
+
+bool stater_server::start(Job &j) {
+    Slot &sl = slots[j.slot];
+    if (cudaMallocAsync((void **)&j.base, j.L.total, sl.stream) != cudaSuccess) {
+        cudaGetLastError();
+        j.base = nullptr;
+        return false;
+    }
+    if (cudaMemsetAsync(j.base, 0, j.L.off_samples, sl.stream) != cudaSuccess) return false;
+    if (cudaEventCreateWithFlags(&j.ev, cudaEventDisableTiming) != cudaSuccess) return false;
+    if (!enqueue_round(j, j.d.spp, true)) return false;
+    return enqueue_after_round(j);
+}
+
+void stater_server::finish(Job &j, bool ok) {
+    if (j.slot >= 0) {
+        Slot &sl = slots[j.slot];
+        if (j.base) cudaFreeAsync(j.base, sl.stream);
+        if (!ok) cudaStreamSynchronize(sl.stream);
+        sl.busy = false;
+    }
+    if (j.ev) cudaEventDestroy(j.ev);
+    j.ev = nullptr;
+    j.base = nullptr;
+    j.t_done = Clock::now();
+    j.latency_ms = std::chrono::duration<double, std::milli>(j.t_done - j.t_submit).count();
+    std::lock_guard<std::mutex> lk(mu);
+    used -= j.footprint;
+    j.state = ok ? STATER_JOB_DONE : STATER_JOB_FAILED;
+    if (ok) {
+        completed++;
+        latencies.push_back(j.latency_ms);
+        pixels_done += (double)j.L.HW;
+        last_done = j.t_done;
+    } else {
+        failed++;
+    }
+    active.erase(std::remove_if(active.begin(), active.end(), [&](const std::shared_ptr<Job> &p) { return p.get() == &j; }),
+                 active.end());
+    cv_done.notify_all();
+}
+
+// Scheduler loop: admit queued jobs in arrival order while a slot is free and
+// the head job's footprint fits under the budget, then advance every job whose
+// event has completed.
+void stater_server::run() {
+    cudaSetDevice(device);
+    while (true) {
+        std::vector<std::shared_ptr<Job>> to_start;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            if (stop && queue.empty() && active.empty()) break;
+            while (!queue.empty()) {
+                auto &j = queue.front();
+                int free_slot = -1;
+                for (size_t i = 0; i < slots.size(); i++)
+                    if (!slots[i].busy) {
+                        free_slot = (int)i;
+                        break;
+                    }
+                const bool fits = used + j->footprint <= budget || active.empty();
+                if (free_slot < 0 || !fits) break;
+                slots[free_slot].busy = true;
+                j->slot = free_slot;
+                j->state = STATER_JOB_RUNNING;
+                used += j->footprint;
+                peak = std::max(peak, used);
+                active.push_back(j);
+                to_start.push_back(j);
+                queue.pop_front();
+            }
+        }
+        for (auto &j : to_start)
+            if (!start(*j)) finish(*j, false);
+        bool progressed = !to_start.empty();
+        std::vector<std::shared_ptr<Job>> snapshot;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            snapshot = active;
+        }
+        for (auto &j : snapshot) {
+            if (!j->ev) continue;
+            const cudaError_t q = cudaEventQuery(j->ev);
+            if (q == cudaErrorNotReady) continue;
+            progressed = true;
+            if (q != cudaSuccess) {
+                cudaGetLastError();
+                finish(*j, false);
+                continue;
+            }
+            if (j->final_enqueued) {
+                finish(*j, true);
+                continue;
+            }
+            // the previous round's largest per-pixel target is now in pinned memory
+            const int next = *slots[j->slot].hmax;
+            bool ok = enqueue_round(*j, next, false) && enqueue_after_round(*j);
+            if (!ok) finish(*j, false);
+        }
+        if (!progressed) {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_work.wait_for(lk, std::chrono::microseconds(50));
+        }
+    }
+}
+
+extern "C" {
+
+double stater_job_footprint(const stater_job_desc *job, int32_t precision, int32_t chunk_spp) {
+    if (!job) return 0;
+    const Layout L = layout(*job, precision, chunk_spp);
+    return (double)L.total + (double)scratch_bytes(L);
+}
+
+stater_status stater_server_create(const stater_server_config *cfg, stater_server **out) {
+    clear_error();
+    if (!cfg || !out || cfg->max_slots < 1 || cfg->max_slots > 64 ||
+        (cfg->precision != STATER_F32 && cfg->precision != STATER_F64))
+        return set_error(STATER_ERR_INVALID, "stater_server_create: bad configuration");
+    auto *s = new stater_server();
+    s->cfg = *cfg;
+    if (s->cfg.chunk_spp <= 0) s->cfg.chunk_spp = 32;
+    cudaGetDevice(&s->device);
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    s->budget = cfg->hbm_budget_bytes > 0 ? cfg->hbm_budget_bytes : 0.8 * (double)free_b;
+    // keep freed job memory in the pool instead of returning it to the driver
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, s->device) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    s->slots.resize(cfg->max_slots);
+    for (auto &sl : s->slots) {
+        if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaMallocHost(&sl.hmax, sizeof(int32_t)) != cudaSuccess) {
+            cudaGetLastError();
+            delete s;
+            return set_error(STATER_ERR_CUDA, "stater_server_create: stream or pinned allocation failed");
+        }
+    }
+    s->worker = std::thread([s] { s->run(); });
+    *out = s;
+    return STATER_OK;
+}
+
+stater_status stater_server_submit(stater_server *srv, const stater_job_desc *job, int64_t *job_id) {
+    clear_error();
+    if (!srv || !job || job->width <= 0 || job->height <= 0 || job->spp < 1 || job->rounds < 1 ||
+        job->n_transforms < 1 || job->n_transforms > STATER_MAX_TRANSFORMS ||
+        job->transforms[0].kind != STATER_TK_IDENTITY || job->n_features < 0 ||
+        job->n_features > STATER_MAX_FEATURES || job->max_moment < 3 || job->max_moment > 5 ||
+        job->filter_radius < 0 || job->filter_radius > STATER_MAX_RADIUS || !(job->filter_sd > 0.f) ||
+        !(job->alpha > 0.f && job->alpha < 1.f))
+        return set_error(STATER_ERR_INVALID, "stater_server_submit: bad job description");
+    if (srv->cfg.precision == STATER_F64 && job->out_host)
+        return set_error(STATER_ERR_UNSUPPORTED, "stater_server_submit: host output is float32 (serve in STATER_F32)");
+    auto j = std::make_shared<Job>();
+    j->d = *job;
+    j->L = layout(*job, srv->cfg.precision, srv->cfg.chunk_spp);
+    j->footprint = (double)j->L.total + (double)scratch_bytes(j->L);
+    j->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        if (j->footprint > srv->budget)
+            return set_error(STATER_ERR_NOMEM, "stater_server_submit: the job alone exceeds the memory budget");
+        j->id = srv->next_id++;
+        srv->jobs[j->id] = j;
+        srv->queue.push_back(j);
+        srv->submitted++;
+        if (!srv->have_first) {
+            srv->have_first = true;
+            srv->first_submit = j->t_submit;
+        }
+    }
+    srv->cv_work.notify_all();
+    if (job_id) *job_id = j->id;
+    return STATER_OK;
+}
+
+stater_status stater_server_poll(stater_server *srv, int64_t job_id, int32_t *state, double *latency_ms) {
+    clear_error();
+    if (!srv) return set_error(STATER_ERR_INVALID, "stater_server_poll: null server");
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto it = srv->jobs.find(job_id);
+    if (it == srv->jobs.end()) return set_error(STATER_ERR_INVALID, "stater_server_poll: unknown job");
+    if (state) *state = it->second->state;
+    if (latency_ms) *latency_ms = it->second->latency_ms;
+    return STATER_OK;
+}
+
+stater_status stater_server_wait(stater_server *srv, int64_t job_id, double timeout_s) {
+    clear_error();
+    if (!srv) return set_error(STATER_ERR_INVALID, "stater_server_wait: null server");
+    std::unique_lock<std::mutex> lk(srv->mu);
+    auto it = srv->jobs.find(job_id);
+    if (it == srv->jobs.end()) return set_error(STATER_ERR_INVALID, "stater_server_wait: unknown job");
+    auto j = it->second;
+    const bool ok = srv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), [&] {
+        return j->state == STATER_JOB_DONE || j->state == STATER_JOB_FAILED;
+    });
+    if (!ok) return set_error(STATER_ERR_TIMEOUT, "stater_server_wait: job not finished in time");
+    if (j->state == STATER_JOB_FAILED) return set_error(STATER_ERR_CUDA, "stater_server_wait: job failed");
+    return STATER_OK;
+}
+
+stater_status stater_server_drain(stater_server *srv, double timeout_s) {
+    clear_error();
+    if (!srv) return set_error(STATER_ERR_INVALID, "stater_server_drain: null server");
+    std::unique_lock<std::mutex> lk(srv->mu);
+    const bool ok = srv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s),
+                                          [&] { return srv->queue.empty() && srv->active.empty(); });
+    return ok ? STATER_OK : set_error(STATER_ERR_TIMEOUT, "stater_server_drain: jobs still running");
+}
+
+stater_status stater_server_stats_get(stater_server *srv, stater_server_stats *out) {
+    clear_error();
+    if (!srv || !out) return set_error(STATER_ERR_INVALID, "stater_server_stats_get: null argument");
+    std::lock_guard<std::mutex> lk(srv->mu);
+    std::memset(out, 0, sizeof(*out));
+    out->submitted = srv->submitted;
+    out->completed = srv->completed;
+    out->failed = srv->failed;
+    out->running = (int64_t)srv->active.size();
+    out->queued = (int64_t)srv->queue.size();
+    out->peak_footprint_bytes = srv->peak;
+    if (!srv->latencies.empty()) {
+        std::vector<double> v = srv->latencies;
+        std::sort(v.begin(), v.end());
+        auto pct = [&](double q) {
+            const double pos = q * (double)(v.size() - 1);
+            const size_t i = (size_t)pos;
+            const double f = pos - (double)i;
+            return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
+        };
+        out->latency_p50_ms = pct(0.50);
+        out->latency_p99_ms = pct(0.99);
+        double sum = 0;
+        for (double x : v) sum += x;
+        out->latency_mean_ms = sum / (double)v.size();
+        const double span = std::chrono::duration<double>(srv->last_done - srv->first_submit).count();
+        out->mpix_per_s = span > 0 ? srv->pixels_done / span / 1e6 : 0;
+    }
+    return STATER_OK;
+}
+
+stater_status stater_server_destroy(stater_server *srv) {
+    clear_error();
+    if (!srv) return STATER_OK;
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        srv->stop = true;
+    }
+    srv->cv_work.notify_all();
+    if (srv->worker.joinable()) srv->worker.join();
+    for (auto &sl : srv->slots) {
+        if (sl.stream) {
+            cudaStreamSynchronize(sl.stream);
+            cudaStreamDestroy(sl.stream);
+        }
+        if (sl.hmax) cudaFreeHost(sl.hmax);
+    }
+    delete srv;
+    return STATER_OK;
+}
+
+}  // extern "C"
