@@ -156,6 +156,7 @@ typedef struct {
     float firefly_prob, firefly_scale;
     float lev_r2;               /* 0 = off */
     const int32_t *first_index; /* nullable */
+    const int32_t *count;       /* nullable: only the first count[p] samples of pixel p are written */
     float *samples;
 } stater_generate_args;
 stater_status stater_generate_samples(const stater_generate_args *a, stater_stream stream);
@@ -308,7 +309,7 @@ stater_status stater_lev_solve(int32_t width, int32_t height, int32_t n_features
  * them, runs denoiseVars and denoiseFilm, and copies the denoised film to
  * `out_host`. With rounds > 1 a job is rendered adaptively: after each round its
  * moment buffers stay on the device, calcTargetSPP allots the next round's
- * samples (spp on average per pixel, clamped to [16, 1024]) and the round's
+ * samples (round_spp on average per pixel, clamped to [16, 1024]) and the round's
  * samples continue every pixel's own sample sequence. Results are independent of
  * what else runs: a job gives the same output alone and in any mix. */
 typedef struct stater_server stater_server;
@@ -322,8 +323,9 @@ typedef struct {
 
 typedef struct {
     int32_t width, height;
-    int32_t spp;                /* samples per pixel (first round, and average per later round) */
+    int32_t spp;                /* samples per pixel of the first round */
     int32_t rounds;             /* 1 = one pass */
+    int32_t round_spp;          /* average extra samples per pixel in each later round (0 = spp) */
     int32_t n_transforms;
     stater_transform transforms[STATER_MAX_TRANSFORMS];
     int32_t n_features;         /* feature channels generated; the range kernels use albedo (0-2, sigma 0.02),

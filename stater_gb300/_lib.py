@@ -53,7 +53,7 @@ class GenerateArgs(C.Structure):
                 ("n_features", C.c_int32), ("seed", C.c_uint64), ("region", C.c_int32),
                 ("mean_mu", C.c_float), ("mean_sigma", C.c_float), ("noise_sigma", C.c_float),
                 ("firefly_prob", C.c_float), ("firefly_scale", C.c_float), ("lev_r2", C.c_float),
-                ("first_index", VP), ("samples", VP)]
+                ("first_index", VP), ("count", VP), ("samples", VP)]
 
 
 class DenoiseVarsArgs(C.Structure):

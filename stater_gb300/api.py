@@ -195,8 +195,8 @@ def bits_words(radius: int) -> int:
 def generate_samples(width: int, height: int, n_samples: int, n_features: int = 7, seed: int = 0,
                      region: int = 8, mean_mu: float = -1.0, mean_sigma: float = 1.0, noise_sigma: float = 0.5,
                      firefly_prob: float = 1e-3, firefly_scale: float = 1e3, lev_r2: float = 0.0,
-                     first_index: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None,
-                     device="cuda", stream=None) -> torch.Tensor:
+                     first_index: Optional[torch.Tensor] = None, count: Optional[torch.Tensor] = None,
+                     out: Optional[torch.Tensor] = None, device="cuda", stream=None) -> torch.Tensor:
     """Seeded synthetic sample planes [S, 5+G, H, W] generated on the device."""
     if out is None:
         out = torch.empty(n_samples, 5 + n_features, height, width, dtype=torch.float32, device=device)
@@ -205,7 +205,7 @@ def generate_samples(width: int, height: int, n_samples: int, n_features: int = 
     g.seed, g.region = int(seed), int(region)
     g.mean_mu, g.mean_sigma, g.noise_sigma = mean_mu, mean_sigma, noise_sigma
     g.firefly_prob, g.firefly_scale, g.lev_r2 = firefly_prob, firefly_scale, lev_r2
-    g.first_index, g.samples = _ptr(first_index), _ptr(out)
+    g.first_index, g.count, g.samples = _ptr(first_index), _ptr(count), _ptr(out)
     L.call("stater_generate_samples", C.byref(g), _stream_ptr(stream))
     return out
 

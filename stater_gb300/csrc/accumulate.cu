@@ -19,6 +19,7 @@ struct GenParams {
     uint32_t k0, k1;
     float mean_mu, mean_sigma, noise_sigma, ff_prob, ff_scale, lev_r2, lev_b;
     const int32_t *first_index;
+    const int32_t *count;
     float *samples;
 };
 
@@ -58,7 +59,8 @@ __global__ void generate_kernel(GenParams g) {
         for (int j = 0; j < 4 && f + j < g.G; j++) base[f + j] = u01(v[j]);
     }
 
-    for (int s = 0; s < g.S; s++) {
+    const int ns = g.count ? min(max(g.count[p], 0), g.S) : g.S;
+    for (int s = 0; s < ns; s++) {
         const uint32_t sidx = first + (uint32_t)s;
         float *out = g.samples + (size_t)s * NCH * HW + p;
         const U4 a = philox4x32_10({(uint32_t)p, sidx, 0u, 0u}, g.k0, g.k1);
@@ -281,6 +283,7 @@ stater_status stater_generate_samples(const stater_generate_args *a, stater_stre
         g.lev_b = (float)std::sqrt((1.0 - r2) / r2 * (1.0 / 48.0) / var_ln);
     }
     g.first_index = a->first_index;
+    g.count = a->count;
     g.samples = a->samples;
     const size_t HW = (size_t)g.W * g.H;
     generate_kernel<<<(unsigned)((HW + 255) / 256), 256, 0, (cudaStream_t)stream>>>(g);

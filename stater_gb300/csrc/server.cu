@@ -198,6 +198,7 @@ bool stater_server::enqueue_round(Job &j, int samples, bool uniform) {
         g.firefly_prob = 1e-3f;
         g.firefly_scale = 1e3f;
         g.first_index = n;  // every pixel continues its own sample sequence
+        g.count = uniform ? nullptr : counts;  // only the samples the accumulation will read
         g.samples = smp;
         if (stater_generate_samples(&g, (stater_stream)s) != STATER_OK) return false;
         stater_accumulate_args a{};
@@ -261,7 +262,8 @@ bool stater_server::enqueue_after_round(Job &j) {
     j.round++;
     if (j.round < j.d.rounds) {
         int32_t *target = (int32_t *)(j.base + L.off_target);
-        if (stater_calc_target_spp(j.d.width, j.d.height, j.d.spp, prec_of(this), v.n, v.varD[0], moment(0, STATER_Q_MEAN),
+        const int budget = j.d.round_spp > 0 ? j.d.round_spp : j.d.spp;
+        if (stater_calc_target_spp(j.d.width, j.d.height, budget, prec_of(this), v.n, v.varD[0], moment(0, STATER_Q_MEAN),
                                    kEps, kTmin, kTmax, target, (stater_stream)s) != STATER_OK)
             return false;
         int32_t *dmax = (int32_t *)(j.base + L.off_max);
@@ -458,7 +460,7 @@ stater_status stater_server_submit(stater_server *srv, const stater_job_desc *jo
         job->transforms[0].kind != STATER_TK_IDENTITY || job->n_features < 0 ||
         job->n_features > STATER_MAX_FEATURES || job->max_moment < 3 || job->max_moment > 5 ||
         job->filter_radius < 0 || job->filter_radius > STATER_MAX_RADIUS || !(job->filter_sd > 0.f) ||
-        !(job->alpha > 0.f && job->alpha < 1.f))
+        !(job->alpha > 0.f && job->alpha < 1.f) || job->round_spp < 0)
         return set_error(STATER_ERR_INVALID, "stater_server_submit: bad job description");
     if (srv->cfg.precision == STATER_F64 && job->out_host)
         return set_error(STATER_ERR_UNSUPPORTED, "stater_server_submit: host output is float32 (serve in STATER_F32)");

@@ -17,7 +17,7 @@ class ServerConfig(C.Structure):
 
 class JobDesc(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("rounds", C.c_int32),
-                ("n_transforms", C.c_int32), ("transforms", L.Transform * L.MAX_TRANSFORMS),
+                ("round_spp", C.c_int32), ("n_transforms", C.c_int32), ("transforms", L.Transform * L.MAX_TRANSFORMS),
                 ("n_features", C.c_int32), ("max_moment", C.c_int32), ("filter_radius", C.c_int32),
                 ("filter_sd", C.c_float), ("alpha", C.c_float), ("var_z", C.c_float), ("seed", C.c_uint64),
                 ("out_host", C.c_void_p)]
@@ -58,11 +58,11 @@ def _bind():
 
 
 def job_desc(width: int, height: int, spp: int, transforms: Sequence = ("identity", "log1p", "sqrt", "cbrt", "asinh"),
-             rounds: int = 1, n_features: int = 7, max_moment: int = 3, radius: int = 10, filter_sd: float = 10.0,
+             rounds: int = 1, round_spp: int = 0, n_features: int = 7, max_moment: int = 3, radius: int = 10, filter_sd: float = 10.0,
              alpha: float = 0.01, var_z: float = 2.80703, seed: int = 0,
              out: Optional[np.ndarray] = None) -> JobDesc:
     d = JobDesc()
-    d.width, d.height, d.spp, d.rounds = width, height, spp, rounds
+    d.width, d.height, d.spp, d.rounds, d.round_spp = width, height, spp, rounds, round_spp
     codes = transform_codes(transforms)
     d.n_transforms = len(codes)
     for k, (kind, lam) in enumerate(codes):

@@ -67,7 +67,7 @@ def test_same_result_alone_and_in_mix(S):
         assert np.all(np.isfinite(o)) and o.max() > 0
 
 
-def _manual(S, width, height, spp, rounds=1, transforms=BASE_TR, radius=10, seed=0, chunk=32):
+def _manual(S, width, height, spp, rounds=1, round_spp=0, transforms=BASE_TR, radius=10, seed=0, chunk=32):
     b = S.StatBuffers(width, height, transforms, 7, 3, S.F32)
     specs = list(S.GBUFFERS_ALL7)
     target = torch.zeros(height, width, dtype=torch.int32, device="cuda")
@@ -82,7 +82,7 @@ def _manual(S, width, height, spp, rounds=1, transforms=BASE_TR, radius=10, seed
     accumulate(spp, None)
     for r in range(1, rounds):
         b.denoise_vars(radius=radius, gbuffers=specs)
-        b.calc_target_spp(spp, target, relative=True, eps=1e-4, tmin=16, tmax=1024)
+        b.calc_target_spp(round_spp or spp, target, relative=True, eps=1e-4, tmin=16, tmax=1024)
         accumulate(int(target.max().item()), target)
     b.denoise_vars(radius=radius, gbuffers=specs)
     b.denoise_film(radius=radius, gbuffers=specs)
@@ -90,10 +90,11 @@ def _manual(S, width, height, spp, rounds=1, transforms=BASE_TR, radius=10, seed
     return b.filmD.cpu().numpy()
 
 
-@pytest.mark.parametrize("rounds", [1, 3])
-def test_server_equals_manual_pipeline(S, rounds):
+@pytest.mark.parametrize("rounds,round_spp", [(1, 0), (3, 0), (4, 64)])
+def test_server_equals_manual_pipeline(S, rounds, round_spp):
     from stater_gb300 import serving
-    kw = dict(width=144, height=88, spp=40, rounds=rounds, radius=6, seed=11)
+    kw = dict(width=144, height=88, spp=16 if round_spp else 40, rounds=rounds, round_spp=round_spp, radius=6,
+              seed=11)
     out = _run_alone(serving, kw)
     ref = _manual(S, **kw)
     assert np.array_equal(out, ref)
