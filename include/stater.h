@@ -274,6 +274,41 @@ stater_status stater_calc_target_spp_noalloc(int32_t width, int32_t height, int3
                                              int32_t tmin, int32_t tmax, int32_t *targetspp,
                                              stater_stream stream);
 
+/* ---- film buffer --------------------------------------------------------- */
+
+/* FilmTile::AddSample with the box filter of radius 0.5 (core/film.h:152-190;
+ * the statistics integrator forces that filter, core/api.cpp:1713-1739) for
+ * whole sample planes as stater_accumulate reads them (R, G, B, u, v first).
+ * Radiance above max_sample_luminance (luminance per core/spectrum.h:483-486) is
+ * scaled down to it, as FilmTile does (+inf: off, the reference's default). Each
+ * pixel's own samples are summed in order into contrib_sum (RGB planes) and
+ * weight_sum, which persist across calls like the reference's film tiles do
+ * across iterations (statpath.cpp:144, 388). A sample on a pixel edge (u or v
+ * exactly 0 or 1) also lies in the neighbour's filter support and is added to
+ * that neighbour's spill planes (R, G, B, weight) by atomic adds, so several
+ * edge samples landing on one pixel are summed in no fixed order. Zero the three
+ * buffers to start a film (Film::Clear with fresh tiles). Device pointers. */
+typedef struct {
+    int32_t width, height;
+    int32_t n_samples;          /* S */
+    int32_t n_features;         /* G: sample planes [S][5+G][W*H] */
+    const float *samples;
+    const int32_t *count;       /* nullable: first count[p] samples of pixel p */
+    float max_sample_luminance; /* FilmTile maxSampleLuminance; INFINITY = off */
+    float *contrib_sum;         /* [3][W*H] */
+    float *weight_sum;          /* [W*H] */
+    float *spill;               /* [4][W*H] */
+} stater_film_args;
+stater_status stater_film_add_samples(const stater_film_args *a, stater_stream stream);
+
+/* Film::UpdateImage (core/film.cpp:187-222) without splats: xyz = RGBToXYZ(own
+ * sum) + RGBToXYZ(spill) (the MergeFilmTile sums, film.cpp:140-149), film RGB =
+ * max(0, XYZToRGB(xyz) / weight) where the weight is non-zero, times scale. This
+ * is the `film` input of stater_denoise_film. spill may be NULL. float RGB planes. */
+stater_status stater_film_update_image(int32_t width, int32_t height, const float *contrib_sum,
+                                       const float *weight_sum, const float *spill, float scale,
+                                       float *rgb, stater_stream stream);
+
 /* Estimator::CalcMeanVars / calcMatMeanVar (estimator.cpp:462-496):
  * meanVar = m2 / ((n - 1) * n) in float arithmetic. RGB buffers. */
 stater_status stater_calc_mean_var(int32_t width, int32_t height, const int32_t *n,

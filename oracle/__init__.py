@@ -210,3 +210,37 @@ def lev_solve(state, G, H, W, lam=1e-6, nthreads=None):
     lib.orc_lev_solve_f64(W, H, G, _p(_c(state, np.float64)), C.c_double(lam), _p(beta), _p(m2C), _p(r2),
                           nthreads or threads())
     return {"beta": beta, "m2C": m2C, "r2": r2}
+
+
+def film_constants():
+    """(RGB->XYZ 3x3, XYZ->RGB 3x3, luminance weights 3) as the oracle uses them."""
+    lib = load()
+    a = np.zeros((3, 3), np.float32)
+    b = np.zeros((3, 3), np.float32)
+    y = np.zeros(3, np.float32)
+    lib.orc_film_constants(_p(a), _p(b), _p(y))
+    return a, b, y
+
+
+def film_add_samples(samples, count=None, max_lum=np.inf, state=None):
+    """FilmTile::AddSample over sample planes [S][5+G][H][W]. state = (contrib_sum
+    [3,H,W], weight_sum [H,W], spill [4,H,W]) continued in place; new if None."""
+    lib = load()
+    samples = _c(samples, np.float32)
+    S, NCH, H, W = samples.shape
+    if state is None:
+        state = (np.zeros((3, H, W), np.float32), np.zeros((H, W), np.float32), np.zeros((4, H, W), np.float32))
+    cs, ws, sp = state
+    cnt = None if count is None else _c(count, np.int32)
+    lib.orc_film_add_samples(W, H, NCH - 5, S, _p(samples), _p(cnt), C.c_float(max_lum), _p(cs), _p(ws), _p(sp))
+    return state
+
+
+def film_update_image(state, scale=1.0):
+    """Film::UpdateImage: film RGB [3,H,W] from film_add_samples' state."""
+    lib = load()
+    cs, ws, sp = state
+    H, W = ws.shape
+    rgb = np.zeros((3, H, W), np.float32)
+    lib.orc_film_update_image(W, H, _p(cs), _p(ws), _p(sp), C.c_float(scale), _p(rgb))
+    return rgb

@@ -814,3 +814,100 @@ void orc_lev_solve_f64(int W, int H, int G, const double *state, double lambda, 
     c.beta = beta; c.m2C = m2C; c.r2 = r2;
     parallel_for((int64_t)W * H, nthreads, lev_solve_range, &c);
 }
+
+/* ---------------------------------------------------------------------------
+ * Film path: FilmTile::AddSample with the box filter of radius 0.5
+ * (core/film.h:152-190; filter width forced in core/api.cpp:1713-1739) and
+ * Film::UpdateImage (core/film.cpp:187-222), colour matrices of
+ * core/spectrum.h:66-76, luminance weights of core/spectrum.h:483-486.
+ * ------------------------------------------------------------------------- */
+static const float kRgbToXyz[3][3] = {{0.412453f, 0.357580f, 0.180423f},
+                                      {0.212671f, 0.715160f, 0.072169f},
+                                      {0.019334f, 0.119193f, 0.950227f}};
+static const float kXyzToRgb[3][3] = {{3.240479f, -1.537150f, -0.498535f},
+                                      {-0.969256f, 1.875991f, 0.041556f},
+                                      {0.055648f, -0.204043f, 1.057311f}};
+static const float kYWeight[3] = {0.212671f, 0.715160f, 0.072169f};
+
+void orc_film_constants(float *rgb_to_xyz, float *xyz_to_rgb, float *y_weight) {
+    memcpy(rgb_to_xyz, kRgbToXyz, sizeof(kRgbToXyz));
+    memcpy(xyz_to_rgb, kXyzToRgb, sizeof(kXyzToRgb));
+    memcpy(y_weight, kYWeight, sizeof(kYWeight));
+}
+
+/* The box filter's support of a sample at pFilm = pixel + (u, v) covers pixels
+ * ceil(x + u - 1) .. floor(x + u) (film.h:158-161 with radius 0.5): the own
+ * pixel, plus the left one when u == 0 and the right one when u == 1 (same in
+ * y). Every covered pixel inside the image gets weight 1 (BoxFilter::Evaluate).
+ * Samples of pixel p go to contrib_sum/weight_sum of p in sample order; those
+ * that also cover a neighbour q are summed into spill of q, visiting pixels in
+ * row-major order and their samples in order. */
+void orc_film_add_samples(int W, int H, int G, int S, const float *samples, const int32_t *count,
+                          float max_lum, float *contrib_sum, float *weight_sum, float *spill) {
+    const size_t HW = (size_t)W * H;
+    const size_t NCH = 5 + (size_t)G;
+    for (size_t p = 0; p < HW; p++) {
+        const int x = (int)(p % W), y = (int)(p / W);
+        int cnt = count ? count[p] : S;
+        if (cnt < 0) cnt = 0;
+        if (cnt > S) cnt = S;
+        for (int s = 0; s < cnt; s++) {
+            const float *sp = samples + (size_t)s * NCH * HW + p;
+            float L[3] = {sp[0], sp[HW], sp[2 * HW]};
+            const float u = sp[3 * HW], v = sp[4 * HW];
+            const float lum = kYWeight[0] * L[0] + kYWeight[1] * L[1] + kYWeight[2] * L[2];
+            if (lum > max_lum) {
+                const float f = max_lum / lum;
+                for (int c = 0; c < 3; c++) L[c] = L[c] * f;
+            }
+            for (int c = 0; c < 3; c++) contrib_sum[c * HW + p] = contrib_sum[c * HW + p] + L[c];
+            weight_sum[p] = weight_sum[p] + 1.0f;
+            const int dx0 = u == 0.0f ? -1 : 0, dx1 = u == 1.0f ? 1 : 0;
+            const int dy0 = v == 0.0f ? -1 : 0, dy1 = v == 1.0f ? 1 : 0;
+            for (int dy = dy0; dy <= dy1; dy++)
+                for (int dx = dx0; dx <= dx1; dx++) {
+                    if (dx == 0 && dy == 0) continue;
+                    const int qx = x + dx, qy = y + dy;
+                    if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
+                    const size_t q = (size_t)qy * W + qx;
+                    for (int c = 0; c < 3; c++) spill[c * HW + q] = spill[c * HW + q] + L[c];
+                    spill[3 * HW + q] = spill[3 * HW + q] + 1.0f;
+                }
+        }
+    }
+}
+
+static void rgb_to_xyz(const float *rgb, float *xyz) {
+    for (int i = 0; i < 3; i++)
+        xyz[i] = kRgbToXyz[i][0] * rgb[0] + kRgbToXyz[i][1] * rgb[1] + kRgbToXyz[i][2] * rgb[2];
+}
+
+/* Film::UpdateImage without splats (the statistics integrator splats nothing):
+ * xyz = RGBToXYZ(own sum) + RGBToXYZ(spill), as MergeFilmTile adds each tile's
+ * converted sum (film.cpp:140-149); rgb = max(0, XYZToRGB(xyz) / w) when w != 0;
+ * times scale. */
+void orc_film_update_image(int W, int H, const float *contrib_sum, const float *weight_sum,
+                           const float *spill, float scale, float *rgb) {
+    const size_t HW = (size_t)W * H;
+    for (size_t p = 0; p < HW; p++) {
+        float own[3], sp[3], a[3], b[3], xyz[3], out[3];
+        for (int c = 0; c < 3; c++) {
+            own[c] = contrib_sum[c * HW + p];
+            sp[c] = spill ? spill[c * HW + p] : 0.0f;
+        }
+        rgb_to_xyz(own, a);
+        rgb_to_xyz(sp, b);
+        for (int i = 0; i < 3; i++) xyz[i] = (0.0f + a[i]) + b[i];
+        for (int i = 0; i < 3; i++)
+            out[i] = kXyzToRgb[i][0] * xyz[0] + kXyzToRgb[i][1] * xyz[1] + kXyzToRgb[i][2] * xyz[2];
+        const float w = weight_sum[p] + (spill ? spill[3 * HW + p] : 0.0f);
+        if (w != 0.0f) {
+            const float inv = 1.0f / w;
+            for (int i = 0; i < 3; i++) {
+                const float t = out[i] * inv;
+                out[i] = 0.0f < t ? t : 0.0f;
+            }
+        }
+        for (int i = 0; i < 3; i++) rgb[i * HW + p] = out[i] * scale;
+    }
+}

@@ -104,6 +104,15 @@ void orc_lev_accumulate_f64(int W, int H, int G, int S, const float *samples, co
 void orc_lev_solve_f64(int W, int H, int G, const double *state, double lambda,
                        double *beta, double *m2C, double *r2, int nthreads);
 
+/* Film path (core/film.h:152-190, core/film.cpp:140-149, 187-222). Buffers
+ * float: contrib_sum [3][HW], weight_sum [HW], spill [4][HW] (R,G,B,weight of
+ * samples lying on an edge shared with the pixel), rgb [3][HW]. */
+void orc_film_constants(float *rgb_to_xyz, float *xyz_to_rgb, float *y_weight);
+void orc_film_add_samples(int W, int H, int G, int S, const float *samples, const int32_t *count,
+                          float max_lum, float *contrib_sum, float *weight_sum, float *spill);
+void orc_film_update_image(int W, int H, const float *contrib_sum, const float *weight_sum,
+                           const float *spill, float scale, float *rgb);
+
 #ifdef __cplusplus
 }
 #endif

@@ -82,6 +82,12 @@ class StaterError(RuntimeError):
 _lib = None
 
 
+class FilmArgs(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("n_samples", C.c_int32),
+                ("n_features", C.c_int32), ("samples", VP), ("count", VP),
+                ("max_sample_luminance", C.c_float), ("contrib_sum", VP), ("weight_sum", VP), ("spill", VP)]
+
+
 def load() -> C.CDLL:
     """Loads libstater.so from the package directory (raises if it is absent)."""
     global _lib
@@ -113,6 +119,8 @@ def load() -> C.CDLL:
         "stater_calc_target_spp_noalloc": (st, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, VP, VP, VP,
                                                 C.c_double, C.c_int32, C.c_int32, VP, VP]),
         "stater_calc_mean_var": (st, [C.c_int32, C.c_int32, VP, VP, VP, VP]),
+        "stater_film_add_samples": (st, [C.POINTER(FilmArgs), VP]),
+        "stater_film_update_image": (st, [C.c_int32, C.c_int32, VP, VP, VP, C.c_float, VP, VP]),
         "stater_lev_state_size": (C.c_int32, [C.c_int32, C.c_int32]),
         "stater_lev_accumulate": (st, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, VP, VP, C.c_int32, VP, VP]),
         "stater_lev_solve": (st, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, VP, C.c_double, VP, VP, VP, VP]),

@@ -226,6 +226,45 @@ def calc_mean_var(width: int, height: int, n: torch.Tensor, m2: torch.Tensor, ou
     L.call("stater_calc_mean_var", width, height, _ptr(n), _ptr(m2), _ptr(out), _stream_ptr(stream))
 
 
+class Film:
+    """The renderer's film (pbrt-v3 Film + FilmTiles with the box filter of radius
+    0.5): per-pixel radiance sums that persist across rounds, and the RGB image
+    Film::UpdateImage makes of them, which denoise_film takes as `film`."""
+
+    def __init__(self, width: int, height: int, n_features: int = 7, max_sample_luminance: float = float("inf"),
+                 scale: float = 1.0, device="cuda"):
+        self.W, self.H, self.G = int(width), int(height), int(n_features)
+        self.max_sample_luminance, self.scale = float(max_sample_luminance), float(scale)
+        dev = torch.device(device)
+        self.contrib_sum = torch.zeros(3, self.H, self.W, dtype=torch.float32, device=dev)
+        self.weight_sum = torch.zeros(self.H, self.W, dtype=torch.float32, device=dev)
+        self.spill = torch.zeros(4, self.H, self.W, dtype=torch.float32, device=dev)
+        self.rgb = torch.zeros(3, self.H, self.W, dtype=torch.float32, device=dev)
+
+    def clear(self) -> None:
+        self.contrib_sum.zero_()
+        self.weight_sum.zero_()
+        self.spill.zero_()
+
+    def add_samples(self, samples: torch.Tensor, count: Optional[torch.Tensor] = None, stream=None) -> None:
+        """FilmTile::AddSample for sample planes [S, 5+G, H, W] (float32)."""
+        if samples.dtype != torch.float32 or not samples.is_contiguous() or \
+                samples.shape[1:] != (5 + self.G, self.H, self.W):
+            raise ValueError("samples must be contiguous float32 [S, 5+G, H, W] of the film's size")
+        a = L.FilmArgs()
+        a.width, a.height, a.n_samples, a.n_features = self.W, self.H, samples.shape[0], self.G
+        a.samples, a.count = _ptr(samples), _ptr(count)
+        a.max_sample_luminance = self.max_sample_luminance
+        a.contrib_sum, a.weight_sum, a.spill = _ptr(self.contrib_sum), _ptr(self.weight_sum), _ptr(self.spill)
+        L.call("stater_film_add_samples", C.byref(a), _stream_ptr(stream))
+
+    def update_image(self, stream=None) -> torch.Tensor:
+        """Film::UpdateImage: writes and returns the film RGB planes [3, H, W]."""
+        L.call("stater_film_update_image", self.W, self.H, _ptr(self.contrib_sum), _ptr(self.weight_sum),
+               _ptr(self.spill), self.scale, _ptr(self.rgb), _stream_ptr(stream))
+        return self.rgb
+
+
 class LevState:
     """Per-pixel LEV accumulation state and the regression outputs."""
 

@@ -21,7 +21,7 @@ LIB = PKG / "libstater.so"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-EXACT_UNITS = ["accumulate.cu", "denoise.cu", "target_spp.cu", "lev.cu"]
+EXACT_UNITS = ["accumulate.cu", "denoise.cu", "target_spp.cu", "lev.cu", "film.cu"]
 FAST_UNITS = ["accumulate_fast.cu", "accumulate_tma.cu", "denoise_fast.cu", "lev_fast.cu", "runtime.cu",
               "server.cu"]
 HOST_UNITS = ["tquantile.cpp"]
