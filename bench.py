@@ -33,7 +33,7 @@ UNIT = "Mpix/s"
 WORKLOAD = dict(width=1920, height=1080, spp=256, transforms=["identity", "log1p", "sqrt", "cbrt", "asinh"],
                 features=7, max_moment=3, radius=10, filter_sd=10.0, alpha=0.01, var_z=2.80703,
                 gbuffers=[(0, 3, 0.02), (3, 3, 0.1), (6, 1, 0.1)])
-LAUNCHES_PER_STEP = 5  # accumulate 1, denoise_vars 2, denoise_film 2
+LAUNCHES_PER_STEP = 6  # accumulate (+ film sums) 1, film image 1, denoise_vars 2, denoise_film 2
 
 
 def _config(extra=None):
@@ -124,11 +124,12 @@ def cpu_pipeline_mpix(samples_host, threads):
     t0 = time.perf_counter()
     oracle.accumulate(samples_host, w["transforms"], w["max_moment"], n, st32, g32, precision="f32",
                       nthreads=threads)
+    film = oracle.film_update_image(oracle.film_add_samples(samples_host)).astype(np.float64)
     st = st32.astype(np.float64)
     gm = g32.astype(np.float64)
     v = oracle.denoise_vars(n, st, gm, w["max_moment"], w["radius"], ds, float(np.float32(w["var_z"])),
                             w["gbuffers"], nthreads=threads)
-    oracle.denoise_film(n, st, v["varD"], v["varCD"], v["jb"], gm, st[0, 0], w["radius"], ds,
+    oracle.denoise_film(n, st, v["varD"], v["varCD"], v["jb"], gm, film, w["radius"], ds,
                         float(np.float32(w["alpha"])), w["gbuffers"], nthreads=threads)
     dt = time.perf_counter() - t0
     return H * W / dt / 1e6, dt
@@ -180,16 +181,22 @@ def _specs(S):
     return [S.GBufferSpec(a, c, sg) for a, c, sg in WORKLOAD["gbuffers"]]
 
 
-def _denoise(S, b, stream=None):
+def _denoise(S, b, film, stream=None):
+    """Film::UpdateImage, then denoiseVars and denoiseFilm of the film image."""
     w = WORKLOAD
+    rgb = film.update_image(stream=stream)
+    if b.precision == S.F64:
+        rgb = rgb.double()
     b.denoise_vars(radius=w["radius"], filter_sd=w["filter_sd"], var_z=w["var_z"], gbuffers=_specs(S), stream=stream)
-    b.denoise_film(radius=w["radius"], filter_sd=w["filter_sd"], alpha=w["alpha"], gbuffers=_specs(S), stream=stream)
+    b.denoise_film(radius=w["radius"], filter_sd=w["filter_sd"], alpha=w["alpha"], gbuffers=_specs(S), film=rgb,
+                   stream=stream)
 
 
-def _reset(b):
+def _reset(b, film):
     b.n.zero_()
     b.stats.zero_()
     b.gmean.zero_()
+    film.clear()
 
 
 def run_gpu(args, rank, world, dist):
@@ -211,32 +218,36 @@ def run_gpu(args, rank, world, dist):
 
     samples = S.generate_samples(W, H, SPP, n_features=G, seed=1234 + rank)
     b = S.StatBuffers(W, H, w["transforms"], G, w["max_moment"], S.F32)
+    film = S.Film(W, H, n_features=G)
 
     def step():
-        _reset(b)
-        b.accumulate(samples, mode=S.ACC_FAST)
-        _denoise(S, b)
+        _reset(b, film)
+        b.accumulate(samples, mode=S.ACC_FAST, film=film)
+        _denoise(S, b, film)
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
 
     # per-stage kernel timings (CUDA events on the launching stream)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-    stage_ms = {"accumulate": [], "denoise_vars": [], "denoise_film": []}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    stage_ms = {"accumulate": [], "film_image": [], "denoise_vars": [], "denoise_film": []}
     for _ in range(3):
-        _reset(b)
+        _reset(b, film)
         ev[0].record(stream)
-        b.accumulate(samples, mode=S.ACC_FAST)
+        b.accumulate(samples, mode=S.ACC_FAST, film=film)
         ev[1].record(stream)
-        b.denoise_vars(radius=w["radius"], filter_sd=w["filter_sd"], var_z=w["var_z"], gbuffers=_specs(S))
+        rgb = film.update_image()
         ev[2].record(stream)
-        b.denoise_film(radius=w["radius"], filter_sd=w["filter_sd"], alpha=w["alpha"], gbuffers=_specs(S))
+        b.denoise_vars(radius=w["radius"], filter_sd=w["filter_sd"], var_z=w["var_z"], gbuffers=_specs(S))
         ev[3].record(stream)
+        b.denoise_film(radius=w["radius"], filter_sd=w["filter_sd"], alpha=w["alpha"], gbuffers=_specs(S), film=rgb)
+        ev[4].record(stream)
         torch.cuda.synchronize()
         stage_ms["accumulate"].append(ev[0].elapsed_time(ev[1]))
-        stage_ms["denoise_vars"].append(ev[1].elapsed_time(ev[2]))
-        stage_ms["denoise_film"].append(ev[2].elapsed_time(ev[3]))
+        stage_ms["film_image"].append(ev[1].elapsed_time(ev[2]))
+        stage_ms["denoise_vars"].append(ev[2].elapsed_time(ev[3]))
+        stage_ms["denoise_film"].append(ev[3].elapsed_time(ev[4]))
 
     # timed region
     steps = args.steps
@@ -262,7 +273,7 @@ def run_gpu(args, rank, world, dist):
     filmD_check = float(b.filmD.double().mean().item())
 
     # roofline of the accumulation kernel (HBM-bound): algorithmic bytes per launch
-    acc_bytes = HW * (SPP * (5 + G) * 4 + 2 * (K * 3 * w["max_moment"] * 4 + G * 4 + 4))
+    acc_bytes = HW * (SPP * (5 + G) * 4 + 2 * (K * 3 * w["max_moment"] * 4 + G * 4 + 4 + 4 * 4))
     acc_ms = statistics.median(stage_ms["accumulate"])
     peaks = {}
     try:
@@ -286,18 +297,19 @@ def run_gpu(args, rank, world, dist):
     # plain FP64 form (one image per launch), same workload
     if not args.no_plain:
         pb = S.StatBuffers(W, H, w["transforms"], G, w["max_moment"], S.F64)
+        pfilm = S.Film(W, H, n_features=G)
         chunk = 32
         samples_c = torch.empty(chunk, 5 + G, H, W, dtype=torch.float32, device="cuda")
         first = torch.zeros(H, W, dtype=torch.int32, device="cuda")
 
         def plain_step(timed_events=None):
-            _reset(pb)
+            _reset(pb, pfilm)
             for c0 in range(0, SPP, chunk):
                 first.fill_(c0)
                 S.generate_samples(W, H, chunk, n_features=G, seed=1234 + rank, first_index=first, out=samples_c)
                 if timed_events is not None:
                     timed_events[0].record(stream)
-                pb.accumulate(samples_c, mode=S.ACC_EXACT)
+                pb.accumulate(samples_c, mode=S.ACC_EXACT, film=pfilm)
                 if timed_events is not None:
                     timed_events[1].record(stream)
                     torch.cuda.synchronize()
@@ -305,7 +317,7 @@ def run_gpu(args, rank, world, dist):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            _denoise(S, pb)
+            _denoise(S, pb, pfilm)
             e1.record(stream)
             torch.cuda.synchronize()
             return e0.elapsed_time(e1)
@@ -322,7 +334,7 @@ def run_gpu(args, rank, world, dist):
                               "accumulate_ms": statistics.median(accs), "denoise_ms": statistics.median(dens),
                               "note": "FP64, one image per launch, sample generation excluded"}
         extra["speedup_vs_plain_f64"] = value / world / extra["plain_f64"]["value"]
-        del pb, samples_c
+        del pb, pfilm, samples_c
         torch.cuda.empty_cache()
 
     # end to end through the public API with pinned host samples
@@ -346,7 +358,7 @@ def run_gpu(args, rank, world, dist):
             e.record(stream)
 
         def e2e_step():
-            _reset(b)
+            _reset(b, film)
             for ci, c0 in enumerate(range(0, SPP, chunk)):
                 s = ci % 2
                 copy_stream.wait_event(free[s])
@@ -354,9 +366,9 @@ def run_gpu(args, rank, world, dist):
                     stage[s].copy_(host[c0:c0 + chunk], non_blocking=True)
                 ready[s].record(copy_stream)
                 stream.wait_event(ready[s])
-                b.accumulate(stage[s], mode=S.ACC_FAST)
+                b.accumulate(stage[s], mode=S.ACC_FAST, film=film)
                 free[s].record(stream)
-            _denoise(S, b)
+            _denoise(S, b, film)
             out_host.copy_(b.filmD, non_blocking=True)
 
         for _ in range(args.warmup):
@@ -377,7 +389,8 @@ def run_gpu(args, rank, world, dist):
             e2e_val = world * HW / (float(t.item()) / 1e3) / 1e6
         e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": SPP * (5 + G) * HW * 4,
                "d2h_bytes_per_step": 3 * HW * 4, "ms_per_step": e2e_ms,
-               "path": "pinned host samples -> 16-spp chunks (copy stream) -> accumulate -> denoise -> filmD to host"}
+               "path": "pinned host samples -> 16-spp chunks (copy stream) -> accumulate + film sums -> film image "
+                       "-> denoise -> filmD to host"}
         del host, stage
         torch.cuda.empty_cache()
 

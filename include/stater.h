@@ -137,6 +137,12 @@ typedef struct {
     int32_t *n;
     void *stats;
     void *gmean;
+    /* Optional film (film_contrib_sum == NULL: off): the same sums as
+     * stater_film_add_samples, taken from the samples this call reads anyway. */
+    float *film_contrib_sum;    /* [3][W*H] */
+    float *film_weight_sum;     /* [W*H] */
+    float *film_spill;          /* [4][W*H] */
+    float film_max_sample_luminance; /* INFINITY = off */
 } stater_accumulate_args;
 stater_status stater_accumulate(const stater_accumulate_args *a, stater_stream stream);
 
@@ -341,8 +347,8 @@ stater_status stater_lev_solve(int32_t width, int32_t height, int32_t n_features
  * the jobs already running, so jobs that arrive while others are on the GPU start
  * without waiting for them and their work overlaps on the device. Each job
  * generates its samples on the device (the seeded synthetic source), accumulates
- * them, runs denoiseVars and denoiseFilm, and copies the denoised film to
- * `out_host`. With rounds > 1 a job is rendered adaptively: after each round its
+ * them together with the film sums, makes the film image (Film::UpdateImage),
+ * runs denoiseVars and denoiseFilm, and copies the denoised film to `out_host`. With rounds > 1 a job is rendered adaptively: after each round its
  * moment buffers stay on the device, calcTargetSPP allots the next round's
  * samples (round_spp on average per pixel, clamped to [16, 1024]) and the round's
  * samples continue every pixel's own sample sequence. Results are independent of

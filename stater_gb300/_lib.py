@@ -45,7 +45,9 @@ class AccumulateArgs(C.Structure):
                 ("n_features", C.c_int32), ("samples", VP), ("count", VP),
                 ("n_transforms", C.c_int32), ("transforms", Transform * MAX_TRANSFORMS),
                 ("max_moment", C.c_int32), ("precision", C.c_int32), ("mode", C.c_int32),
-                ("n", VP), ("stats", VP), ("gmean", VP)]
+                ("n", VP), ("stats", VP), ("gmean", VP),
+                ("film_contrib_sum", VP), ("film_weight_sum", VP), ("film_spill", VP),
+                ("film_max_sample_luminance", C.c_float)]
 
 
 class GenerateArgs(C.Structure):

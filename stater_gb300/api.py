@@ -116,8 +116,9 @@ class StatBuffers:
 
     # -- stage 1 -----------------------------------------------------------------
     def accumulate(self, samples: torch.Tensor, count: Optional[torch.Tensor] = None, mode: int = L.ACC_EXACT,
-                   stream=None) -> None:
-        """StatTile::AddTransformSample* over sample planes [S, 5+G, H, W] (float32)."""
+                   film: Optional["Film"] = None, stream=None) -> None:
+        """StatTile::AddTransformSample* over sample planes [S, 5+G, H, W] (float32);
+        with `film`, also FilmTile::AddSample of the same samples in the same pass."""
         if samples.dtype != torch.float32 or not samples.is_contiguous():
             raise ValueError("samples must be contiguous float32 [S, 5+G, H, W]")
         S = samples.shape[0]
@@ -132,6 +133,11 @@ class StatBuffers:
             a.transforms[k].lambda_ = lam
         a.max_moment, a.precision, a.mode = self.max_moment, self.precision, int(mode)
         a.n, a.stats, a.gmean = _ptr(self.n), _ptr(self.stats), _ptr(self.gmean)
+        if film is not None:
+            if (film.W, film.H, film.G) != (self.W, self.H, self.G):
+                raise ValueError("film geometry does not match the buffers")
+            a.film_contrib_sum, a.film_weight_sum = _ptr(film.contrib_sum), _ptr(film.weight_sum)
+            a.film_spill, a.film_max_sample_luminance = _ptr(film.spill), film.max_sample_luminance
         L.call("stater_accumulate", C.byref(a), _stream_ptr(stream))
 
     # -- stage 2 -----------------------------------------------------------------

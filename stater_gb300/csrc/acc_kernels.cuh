@@ -17,7 +17,7 @@
 #pragma once
 
 #include "common.cuh"
-
+#include "film_common.cuh"
 
 namespace stater {
 
@@ -30,6 +30,9 @@ struct AccParams {
     int32_t *n;
     void *stats;
     void *gmean;
+    // Optional film sums (film.sum == nullptr: off), added by the transform-0
+    // threads from the samples they read anyway.
+    FilmTarget film;
 };
 
 // Compact FP32 forms used by the FAST mode (few instructions, no slow paths;
@@ -175,7 +178,8 @@ __device__ __forceinline__ void feat_update(float v, uint32_t nn, T rn, T &fm) {
 template <typename T, bool FAST, int MAXMOM, int MAXF, int KIND>
 __device__ __forceinline__ void acc_loop(const AccParams &P, size_t p, int k, int cnt, uint32_t n0, float lam,
                                          T (&mean)[3], T (&m2)[3], T (&m3)[3], T (&m4)[3], T (&cx)[3],
-                                         T (&cy)[3], T (&m1)[3], T (&fm)[MAXF > 0 ? MAXF : 1]) {
+                                         T (&cy)[3], T (&m1)[3], T (&fm)[MAXF > 0 ? MAXF : 1], bool film,
+                                         FilmAcc &fa) {
     const size_t HW = P.HW;
     const float *sp = P.samples + p;
     const size_t sstride = (size_t)P.NCH * HW;
@@ -196,6 +200,11 @@ __device__ __forceinline__ void acc_loop(const AccParams &P, size_t p, int k, in
             for (int c = 0; c < NL; c++) nxt[c] = __ldg(spc + sstride + (size_t)c * HW);
         }
         const uint32_t nn = n0 + (uint32_t)s + 1u;
+        if (film) {
+            const float u = NL >= 5 ? cur[NL >= 5 ? 3 : 0] : __ldg(spc + 3 * HW);
+            const float v = NL >= 5 ? cur[NL >= 5 ? 4 : 0] : __ldg(spc + 4 * HW);
+            film_add(P.film, p, cur[0], cur[1], cur[2], u, v, fa);
+        }
         T rn;
         acc_update<T, FAST, MAXMOM, KIND>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
 #pragma unroll
@@ -240,11 +249,15 @@ __global__ void __launch_bounds__(256) acc_kernel(AccParams P) {
         fm[j] = g < P.G ? gm[(size_t)g * HW + p] : T(0);
     }
     const float lam = P.ts.lambda[k];
-    // one specialised sample loop per transform kind (warp-uniform: k = threadIdx.y)
+    // the film sums ride along with transform 0 (warp-uniform: k = threadIdx.y)
+    const bool film = k == 0 && P.film.sum != nullptr;
+    FilmAcc fa{0.f, 0.f, 0.f, 0.f};
+    if (film) film_load(P.film, HW, p, fa);
+    // one specialised sample loop per transform kind (warp-uniform)
     switch (P.ts.kind[k]) {
 #define STATER_ACC_CASE(KD)                                                                                   \
     case KD:                                                                                                  \
-        acc_loop<T, FAST, MAXMOM, MAXF, KD>(P, p, k, cnt, n0, lam, mean, m2, m3, m4, cx, cy, m1, fm);          \
+        acc_loop<T, FAST, MAXMOM, MAXF, KD>(P, p, k, cnt, n0, lam, mean, m2, m3, m4, cx, cy, m1, fm, film, fa); \
         break;
         STATER_ACC_CASE(STATER_TK_LOG1P)
         STATER_ACC_CASE(STATER_TK_SQRT)
@@ -252,9 +265,10 @@ __global__ void __launch_bounds__(256) acc_kernel(AccParams P) {
         STATER_ACC_CASE(STATER_TK_ASINH)
         STATER_ACC_CASE(STATER_TK_BOXCOX)
         default: acc_loop<T, FAST, MAXMOM, MAXF, STATER_TK_IDENTITY>(P, p, k, cnt, n0, lam, mean, m2, m3, m4, cx,
-                                                                     cy, m1, fm);
+                                                                     cy, m1, fm, film, fa);
 #undef STATER_ACC_CASE
     }
+    if (film) film_store(P.film, HW, p, fa);
 
 #pragma unroll
     for (int c = 0; c < 3; c++) {

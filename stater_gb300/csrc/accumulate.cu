@@ -222,6 +222,8 @@ stater_status stater_accumulate(const stater_accumulate_args *a, stater_stream s
     for (int k = 0; k < a->n_transforms; k++)
         if (a->transforms[k].kind < 0 || a->transforms[k].kind > STATER_TK_BOXCOX)
             return set_error(STATER_ERR_INVALID, "stater_accumulate: unknown transform kind");
+    if (a->film_contrib_sum && (!a->film_weight_sum || !a->film_spill || !(a->film_max_sample_luminance > 0.0f)))
+        return set_error(STATER_ERR_INVALID, "stater_accumulate: incomplete film buffers");
     if (a->n_samples == 0) return STATER_OK;
 
     AccParams P;
@@ -239,6 +241,12 @@ stater_status stater_accumulate(const stater_accumulate_args *a, stater_stream s
     P.n = a->n;
     P.stats = a->stats;
     P.gmean = a->gmean;
+    P.film.W = a->width;
+    P.film.H = a->height;
+    P.film.max_lum = a->film_max_sample_luminance;
+    P.film.sum = a->film_contrib_sum;
+    P.film.weight = a->film_weight_sum;
+    P.film.spill = a->film_spill;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e;
     if (a->mode == STATER_ACC_FAST) {

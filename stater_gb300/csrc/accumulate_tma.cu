@@ -165,6 +165,10 @@ __global__ void __launch_bounds__(kPx *STATER_MAX_TRANSFORMS + 32)
     const int kind = P.ts.kind[k];
     const float lam = P.ts.lambda[k];
     constexpr int NL = MAXMOM >= 5 ? 5 : 3;
+    // film sums ride along with the transform-0 warp
+    const bool film = k == 0 && valid && P.film.sum != nullptr;
+    FilmAcc fa{0.f, 0.f, 0.f, 0.f};
+    if (film) film_load(P.film, HW, p, fa);
     bool ok = true;
     for (int c = 0; c < nchunks; c++) {
         const int sidx = c % kStages;
@@ -180,6 +184,7 @@ __global__ void __launch_bounds__(kPx *STATER_MAX_TRANSFORMS + 32)
 #pragma unroll
             for (int q = 0; q < NL; q++) cur[q] = row[q * kPx];
             const uint32_t nn = n0 + (uint32_t)(c * kSB + j) + 1u;
+            if (film) film_add(P.film, p, cur[0], cur[1], cur[2], row[3 * kPx], row[4 * kPx], fa);
             float rn;
             switch (kind) {
                 case STATER_TK_LOG1P:
@@ -232,6 +237,7 @@ __global__ void __launch_bounds__(kPx *STATER_MAX_TRANSFORMS + 32)
         const int g = k + j * P.K;
         if (g < P.G) gm[(size_t)g * HW + p] = fm[j];
     }
+    if (film) film_store(P.film, HW, p, fa);
     if (k == 0) P.n[p] = (int32_t)(n0 + (uint32_t)cnt);
 }
 

@@ -8,6 +8,7 @@
 // Compiled with -fmad=false: every product and sum is rounded on its own, in the
 // order the reference writes them, so the film matches its x86 build bit for bit.
 #include "common.cuh"
+#include "film_common.cuh"
 
 namespace stater {
 namespace {
@@ -25,63 +26,26 @@ __device__ __forceinline__ void xyz_to_rgb(float x, float y, float z, float &r, 
 }
 
 struct FilmParams {
-    int W, H, S, NCH;
+    int S, NCH;
     const float *__restrict__ samples;
     const int32_t *__restrict__ count;
-    float max_lum;
-    float *sum;     // [3][HW]
-    float *weight;  // [HW]
-    float *spill;   // [4][HW]
+    FilmTarget F;
 };
 
-// One thread per pixel, samples in order. The box filter's support of a sample
-// at pFilm = (x + u, y + v) is pixels ceil(x + u - 1) .. floor(x + u): the own
-// pixel, and also the left (right) neighbour exactly when u == 0 (u == 1); the
-// same in y. Those rare edge samples are added to the neighbour's spill planes.
+// One thread per pixel, samples in order; edge samples also go to the
+// neighbours' spill planes (film_common.cuh).
 __global__ void __launch_bounds__(256) film_add_kernel(FilmParams P) {
-    const size_t HW = (size_t)P.W * P.H;
+    const size_t HW = (size_t)P.F.W * P.F.H;
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= HW) return;
-    const int x = (int)(p % (size_t)P.W), y = (int)(p / (size_t)P.W);
     const int cnt = P.count ? min(max(P.count[p], 0), P.S) : P.S;
-    float s0 = P.sum[p], s1 = P.sum[HW + p], s2 = P.sum[2 * HW + p], w = P.weight[p];
+    FilmAcc a;
+    film_load(P.F, HW, p, a);
     const size_t stride = (size_t)P.NCH * HW;
     const float *sp = P.samples + p;
-    for (int s = 0; s < cnt; s++, sp += stride) {
-        float r = __ldg(sp), g = __ldg(sp + HW), b = __ldg(sp + 2 * HW);
-        const float u = __ldg(sp + 3 * HW), v = __ldg(sp + 4 * HW);
-        // FilmTile::AddSample: L *= maxSampleLuminance / L.y() above the limit.
-        const float lum = 0.212671f * r + 0.715160f * g + 0.072169f * b;
-        if (lum > P.max_lum) {
-            const float f = P.max_lum / lum;
-            r = r * f;
-            g = g * f;
-            b = b * f;
-        }
-        s0 = s0 + r;
-        s1 = s1 + g;
-        s2 = s2 + b;
-        w = w + 1.0f;
-        if (u == 0.0f || u == 1.0f || v == 0.0f || v == 1.0f) {
-            const int dx0 = u == 0.0f ? -1 : 0, dx1 = u == 1.0f ? 1 : 0;
-            const int dy0 = v == 0.0f ? -1 : 0, dy1 = v == 1.0f ? 1 : 0;
-            for (int dy = dy0; dy <= dy1; dy++) {
-                for (int dx = dx0; dx <= dx1; dx++) {
-                    const int qx = x + dx, qy = y + dy;
-                    if ((dx == 0 && dy == 0) || qx < 0 || qy < 0 || qx >= P.W || qy >= P.H) continue;
-                    const size_t q = (size_t)qy * P.W + qx;
-                    atomicAdd(P.spill + q, r);
-                    atomicAdd(P.spill + HW + q, g);
-                    atomicAdd(P.spill + 2 * HW + q, b);
-                    atomicAdd(P.spill + 3 * HW + q, 1.0f);
-                }
-            }
-        }
-    }
-    P.sum[p] = s0;
-    P.sum[HW + p] = s1;
-    P.sum[2 * HW + p] = s2;
-    P.weight[p] = w;
+    for (int s = 0; s < cnt; s++, sp += stride)
+        film_add(P.F, p, __ldg(sp), __ldg(sp + HW), __ldg(sp + 2 * HW), __ldg(sp + 3 * HW), __ldg(sp + 4 * HW), a);
+    film_store(P.F, HW, p, a);
 }
 
 // Film::UpdateImage without splats (the statistics integrator splats nothing).
@@ -136,17 +100,17 @@ stater_status stater_film_add_samples(const stater_film_args *a, stater_stream s
         return set_error(STATER_ERR_INVALID, "stater_film_add_samples: max_sample_luminance must be > 0");
     if (a->n_samples == 0) return STATER_OK;
     FilmParams P;
-    P.W = a->width;
-    P.H = a->height;
     P.S = a->n_samples;
     P.NCH = 5 + a->n_features;
     P.samples = a->samples;
     P.count = a->count;
-    P.max_lum = a->max_sample_luminance;
-    P.sum = a->contrib_sum;
-    P.weight = a->weight_sum;
-    P.spill = a->spill;
-    const size_t HW = (size_t)P.W * P.H;
+    P.F.W = a->width;
+    P.F.H = a->height;
+    P.F.max_lum = a->max_sample_luminance;
+    P.F.sum = a->contrib_sum;
+    P.F.weight = a->weight_sum;
+    P.F.spill = a->spill;
+    const size_t HW = (size_t)a->width * a->height;
     film_add_kernel<<<(unsigned)((HW + 255) / 256), 256, 0, (cudaStream_t)stream>>>(P);
     return cuda_status(cudaGetLastError(), "stater_film_add_samples launch");
 }

@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -39,6 +40,11 @@ __global__ void chunk_counts_kernel(size_t HW, const int32_t *target, int done, 
     counts[p] = max(0, min(target[p] - done, chunk));
 }
 
+__global__ void widen_kernel(size_t n, const float *in, double *out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (double)in[i];
+}
+
 __global__ void max_kernel(size_t HW, const int32_t *v, int32_t *out) {
     int m = 0;
     for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < HW; p += (size_t)gridDim.x * blockDim.x)
@@ -51,7 +57,8 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct Layout {
     size_t HW, T, K, G, chunk;
-    size_t off_n, off_counts, off_target, off_max, off_stats, off_gmean, off_jb, off_out6, off_filmD, off_samples, total;
+    size_t off_n, off_counts, off_target, off_max, off_stats, off_gmean, off_film, off_rgb, off_rgb64, off_jb, off_out6,
+        off_filmD, off_samples, total;
 };
 
 int chunk_for(const stater_job_desc &d, int chunk_spp) {
@@ -81,6 +88,9 @@ Layout layout(const stater_job_desc &d, int precision, int chunk_spp) {
     L.off_max = take(4);
     L.off_stats = take(L.K * STATER_NQ * 3 * L.HW * L.T);
     L.off_gmean = take(std::max<size_t>(L.G, 1) * L.HW * L.T);
+    L.off_film = take(8 * L.HW * 4);  // film sums: contrib[3], weight, spill[4]
+    L.off_rgb = take(3 * L.HW * 4);
+    L.off_rgb64 = take(L.T == 8 ? 3 * L.HW * 8 : 0);
     L.off_jb = take(L.K * L.HW * L.T);
     L.off_out6 = take(6 * L.K * 3 * L.HW * L.T);
     L.off_filmD = take(3 * L.HW * L.T);
@@ -216,6 +226,11 @@ bool stater_server::enqueue_round(Job &j, int samples, bool uniform) {
         a.n = n;
         a.stats = j.base + L.off_stats;
         a.gmean = j.base + L.off_gmean;
+        float *fs = (float *)(j.base + L.off_film);
+        a.film_contrib_sum = fs;
+        a.film_weight_sum = fs + 3 * L.HW;
+        a.film_spill = fs + 4 * L.HW;
+        a.film_max_sample_luminance = INFINITY;
         if (stater_accumulate(&a, (stater_stream)s) != STATER_OK) return false;
     }
     return true;
@@ -272,6 +287,19 @@ bool stater_server::enqueue_after_round(Job &j) {
         if (cudaGetLastError() != cudaSuccess) return false;
         if (cudaMemcpyAsync(sl.hmax, dmax, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return false;
     } else {
+        // Film::UpdateImage: the film image is the untransformed mean that denoiseFilm filters
+        const float *fs = (const float *)(j.base + L.off_film);
+        float *rgb = (float *)(j.base + L.off_rgb);
+        if (stater_film_update_image(j.d.width, j.d.height, fs, fs + 3 * L.HW, fs + 4 * L.HW, 1.0f, rgb,
+                                     (stater_stream)s) != STATER_OK)
+            return false;
+        const void *film = rgb;
+        if (L.T == 8) {
+            widen_kernel<<<(unsigned)((3 * L.HW + 255) / 256), 256, 0, s>>>(3 * L.HW, rgb,
+                                                                          (double *)(j.base + L.off_rgb64));
+            if (cudaGetLastError() != cudaSuccess) return false;
+            film = j.base + L.off_rgb64;
+        }
         stater_denoise_film_args f{};
         f.n_buffers = j.d.n_transforms;
         f.width = j.d.width;
@@ -283,7 +311,7 @@ bool stater_server::enqueue_after_round(Job &j) {
         f.use_levc = j.d.max_moment >= 5 ? 1 : 0;
         f.precision = prec_of(this);
         f.n = v.n;
-        f.film = moment(0, STATER_Q_MEAN);
+        f.film = film;
         for (int k = 0; k < j.d.n_transforms; k++) {
             f.mean[k] = moment(k, STATER_Q_MEAN);
             f.varD[k] = v.varD[k];

@@ -117,17 +117,20 @@ class Film {
         a.samples = samples;
         a.count = count;
         a.max_sample_luminance = max_sample_luminance;
-        a.contrib_sum = sum_ptr();
-        a.weight_sum = sum_ptr() + 3 * (size_t)width * height;
-        a.spill = sum_ptr() + 4 * (size_t)width * height;
+        a.contrib_sum = contrib_sum();
+        a.weight_sum = weight_sum();
+        a.spill = spill();
         check(stater_film_add_samples(&a, (stater_stream)s), "Film::AddSamples");
     }
     void UpdateImage(cudaStream_t s) {
-        const size_t HW = (size_t)width * height;
-        check(stater_film_update_image(width, height, sum_ptr(), sum_ptr() + 3 * HW, sum_ptr() + 4 * HW, scale,
+        check(stater_film_update_image(width, height, contrib_sum(), weight_sum(), spill(), scale,
                                        (float *)rgb_.get(), (stater_stream)s),
               "Film::UpdateImage");
     }
+
+    float *contrib_sum() const { return sum_ptr(); }
+    float *weight_sum() const { return sum_ptr() + 3 * (size_t)width * height; }
+    float *spill() const { return sum_ptr() + 4 * (size_t)width * height; }
 
     const int width, height, n_features;
     const float max_sample_luminance, scale;
@@ -199,8 +202,10 @@ class Estimator {
     }
 
     // Stage 1 on the GPU in place of the CPU tiles: every sample of the device
-    // sample planes [S][5+G][H*W] (the first count[p] for pixel p, count may be NULL).
-    void AddSamples(const float *samples, int n_samples, const int32_t *count) {
+    // sample planes [S][5+G][H*W] (the first count[p] for pixel p, count may be
+    // NULL). With `film`, the same pass adds the samples to the film's sums
+    // (Film::AddSamples in one read of the samples).
+    void AddSamples(const float *samples, int n_samples, const int32_t *count, Film *film = nullptr) {
         stater_accumulate_args a;
         std::memset(&a, 0, sizeof(a));
         a.width = width;
@@ -217,6 +222,14 @@ class Estimator {
         a.n = n_ptr();
         a.stats = stats_.get();
         a.gmean = cfg.n_features ? gmean_.get() : nullptr;
+        if (film) {
+            if (film->width != width || film->height != height || film->n_features != cfg.n_features)
+                throw std::invalid_argument("Estimator::AddSamples: film geometry differs");
+            a.film_contrib_sum = film->contrib_sum();
+            a.film_weight_sum = film->weight_sum();
+            a.film_spill = film->spill();
+            a.film_max_sample_luminance = film->max_sample_luminance;
+        }
         check(stater_accumulate(&a, (stater_stream)stream), "Estimator::AddSamples");
     }
 

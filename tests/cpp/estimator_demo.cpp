@@ -3,7 +3,7 @@
 // (statpath.cpp:176-441, 500-560), over libstater.
 //
 //   estimator_demo render <dir> <W> <H> <spp> <seed> <radius>
-//       seeded samples on the device -> Film + Estimator::AddSamples ->
+//       seeded samples on the device -> Estimator::AddSamples (with the film) ->
 //       Film::UpdateImage -> Upload -> DenoiseVars -> DenoiseMeans ->
 //       CalcTargetSPPs -> CalcMeanVars -> Download -> Synchronize, then every
 //       registered buffer written as <dir>/scene-<spp>-<name>.pfm
@@ -72,8 +72,7 @@ static int render(const std::string &dir, int W, int H, int spp, unsigned long l
     check(stater_generate_samples(&g, (stater_stream)est.stream), "generate");
 
     film.Clear(est.stream);
-    film.AddSamples((const float *)samples.get(), spp, nullptr, est.stream);
-    est.AddSamples((const float *)samples.get(), spp, nullptr);
+    est.AddSamples((const float *)samples.get(), spp, nullptr, &film);  // statistics and film in one pass
     film.UpdateImage(est.stream);
 
     est.Upload();

@@ -105,3 +105,39 @@ def test_film_feeds_denoise_film(S):
     assert np.allclose(b.filmD.cpu().numpy(), d["filmD"], rtol=1e-5, atol=0)
     # the film differs from the running mean of the untransformed set
     assert not np.array_equal(orgb.astype(np.float64), so[0, 0])
+
+
+@pytest.mark.parametrize("W,H,precision,mode,mm", [
+    (96, 64, "F32", "ACC_FAST", 3),    # TMA-fed FP32 kernel
+    (97, 61, "F32", "ACC_FAST", 5),    # W*H % 4 != 0: plain FP32 kernel
+    (80, 48, "F32", "ACC_EXACT", 3),
+    (80, 48, "F64", "ACC_EXACT", 5),
+])
+def test_film_fused_into_accumulate(S, W, H, precision, mode, mm):
+    """The film sums taken inside stater_accumulate equal the standalone film pass."""
+    G = 7
+    s1 = synth_samples(W, H, 20, G=G, seed=11)
+    s2 = _edge_samples(W, H, 9, seed=12)
+    s2 = np.concatenate([s2, np.zeros((9, G - 1, H, W), np.float32)], axis=1)
+    c2 = np.random.default_rng(13).integers(0, 10, size=(H, W)).astype(np.int32)
+    b = S.StatBuffers(W, H, ("identity", "log1p", "sqrt"), G, mm, getattr(S, precision))
+    fused = S.Film(W, H, n_features=G, max_sample_luminance=50.0)
+    for smp, cnt in ((s1, None), (s2, c2)):
+        b.accumulate(torch.from_numpy(smp).cuda(), None if cnt is None else torch.from_numpy(cnt).cuda(),
+                     mode=getattr(S, mode), film=fused)
+    rgb = fused.update_image()
+    torch.cuda.synchronize()
+    (oc, ow, os_), orgb = _orc_film([(s1, None), (s2, c2)], max_lum=50.0)
+    assert np.array_equal(fused.contrib_sum.cpu().numpy(), oc)
+    assert np.array_equal(fused.weight_sum.cpu().numpy(), ow)
+    assert np.array_equal(fused.spill[3].cpu().numpy(), os_[3])
+    assert np.allclose(fused.spill.cpu().numpy(), os_, rtol=1e-6, atol=0)
+    single = os_[3] <= 1
+    assert np.array_equal(rgb.cpu().numpy()[:, single], orgb[:, single])
+    # the statistics are those of an accumulation without the film
+    ref = S.StatBuffers(W, H, ("identity", "log1p", "sqrt"), G, mm, getattr(S, precision))
+    for smp, cnt in ((s1, None), (s2, c2)):
+        ref.accumulate(torch.from_numpy(smp).cuda(), None if cnt is None else torch.from_numpy(cnt).cuda(),
+                       mode=getattr(S, mode))
+    torch.cuda.synchronize()
+    assert torch.equal(ref.stats, b.stats) and torch.equal(ref.n, b.n) and torch.equal(ref.gmean, b.gmean)

@@ -69,6 +69,7 @@ def test_same_result_alone_and_in_mix(S):
 
 def _manual(S, width, height, spp, rounds=1, round_spp=0, transforms=BASE_TR, radius=10, seed=0, chunk=32):
     b = S.StatBuffers(width, height, transforms, 7, 3, S.F32)
+    film = S.Film(width, height, 7)
     specs = list(S.GBUFFERS_ALL7)
     target = torch.zeros(height, width, dtype=torch.int32, device="cuda")
 
@@ -77,7 +78,7 @@ def _manual(S, width, height, spp, rounds=1, round_spp=0, transforms=BASE_TR, ra
             n_s = min(chunk, samples - done)
             smp = S.generate_samples(width, height, n_s, n_features=7, seed=seed, region=8, first_index=b.n)
             cnt = None if counts is None else torch.clamp(counts - done, 0, n_s).to(torch.int32).contiguous()
-            b.accumulate(smp, count=cnt, mode=S.ACC_FAST)
+            b.accumulate(smp, count=cnt, mode=S.ACC_FAST, film=film)
 
     accumulate(spp, None)
     for r in range(1, rounds):
@@ -85,7 +86,7 @@ def _manual(S, width, height, spp, rounds=1, round_spp=0, transforms=BASE_TR, ra
         b.calc_target_spp(round_spp or spp, target, relative=True, eps=1e-4, tmin=16, tmax=1024)
         accumulate(int(target.max().item()), target)
     b.denoise_vars(radius=radius, gbuffers=specs)
-    b.denoise_film(radius=radius, gbuffers=specs)
+    b.denoise_film(radius=radius, gbuffers=specs, film=film.update_image())
     torch.cuda.synchronize()
     return b.filmD.cpu().numpy()
 
