@@ -141,7 +141,13 @@ template <typename T, bool FAST, int MAXMOM, int KIND>
 __device__ __forceinline__ void acc_update(const float *cur, uint32_t nn, float lam, T (&mean)[3], T (&m2)[3],
                                            T (&m3)[3], T (&m4)[3], T (&cx)[3], T (&cy)[3], T (&m1)[3], T &rn_out) {
     T rn = T(0);
-    if (FAST) rn = sizeof(T) == 4 ? (T)__frcp_rn((float)nn) : T(1) / (T)nn;  // correctly rounded 1/n
+    if (FAST) {
+        // hardware reciprocal (within 1 ulp): one instruction instead of the
+        // correctly rounded sequence; the first sample never uses it
+        float r;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float)nn));
+        rn = sizeof(T) == 4 ? (T)r : T(1) / (T)nn;
+    }
     rn_out = rn;
     float xD = 0.f, yD = 0.f;
     if (MAXMOM >= 5) {

@@ -25,9 +25,15 @@ bool encode_tensor_map_2d_f32(CUtensorMap *map, const void *base, uint64_t cols,
 
 namespace {
 
-constexpr int kPx = 32;      // pixels per CTA (one warp-wide row of consumers per transform)
-constexpr int kSB = 8;       // samples per stage
-constexpr int kStages = 4;   // ring depth
+#ifndef STATER_TMA_SAMPLES_PER_STAGE
+#define STATER_TMA_SAMPLES_PER_STAGE 4
+#endif
+#ifndef STATER_TMA_STAGES
+#define STATER_TMA_STAGES 4
+#endif
+constexpr int kPx = 32;                                // pixels per CTA (one warp-wide row of consumers per transform)
+constexpr int kSB = STATER_TMA_SAMPLES_PER_STAGE;      // samples per stage
+constexpr int kStages = STATER_TMA_STAGES;             // ring depth
 constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr int kErrTimeout = 1;
 
@@ -75,6 +81,43 @@ struct TmaAccParams {
     AccParams P;
     int *err;
 };
+
+// The consumer loop of one transform kind (the kind is hoisted out of the
+// sample loop: one specialised loop per kind, chosen once per warp). Returns
+// false when a wait gave up.
+template <int MAXMOM, int MAXF, int KIND>
+__device__ __forceinline__ bool tma_consume(const AccParams &P, const float *stages, int stage_floats, uint64_t *full,
+                                            uint64_t *empty, int nchunks, int cnt, uint32_t n0, int k, int lane,
+                                            size_t p, float lam, float (&mean)[3], float (&m2)[3], float (&m3)[3],
+                                            float (&m4)[3], float (&cx)[3], float (&cy)[3], float (&m1)[3],
+                                            float (&fm)[MAXF > 0 ? MAXF : 1], bool film, FilmAcc &fa) {
+    const int NCH = P.NCH;
+    constexpr int NL = MAXMOM >= 5 ? 5 : 3;
+    for (int c = 0; c < nchunks; c++) {
+        const int sidx = c % kStages;
+        if (!mbar_wait(&full[sidx], (c / kStages) & 1)) return false;
+        const float *stage = stages + (size_t)sidx * stage_floats;
+        const int jn = min(kSB, cnt - c * kSB);
+        for (int j = 0; j < jn; j++) {
+            const float *row = stage + (size_t)j * NCH * kPx + lane;
+            float cur[NL];
+#pragma unroll
+            for (int q = 0; q < NL; q++) cur[q] = row[q * kPx];
+            const uint32_t nn = n0 + (uint32_t)(c * kSB + j) + 1u;
+            if (film) film_add(P.film, p, cur[0], cur[1], cur[2], row[3 * kPx], row[4 * kPx], fa);
+            float rn;
+            acc_update<float, true, MAXMOM, KIND>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
+#pragma unroll
+            for (int jf = 0; jf < MAXF; jf++) {
+                const int g = k + jf * P.K;
+                if (g < P.G) feat_update<float, true>(row[(5 + g) * kPx], nn, rn, fm[jf]);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[sidx]);
+    }
+    return true;
+}
 
 template <int MAXMOM, int MAXF>
 __global__ void __launch_bounds__(kPx *STATER_MAX_TRANSFORMS + 32)
@@ -164,56 +207,27 @@ __global__ void __launch_bounds__(kPx *STATER_MAX_TRANSFORMS + 32)
     }
     const int kind = P.ts.kind[k];
     const float lam = P.ts.lambda[k];
-    constexpr int NL = MAXMOM >= 5 ? 5 : 3;
     // film sums ride along with the transform-0 warp
     const bool film = k == 0 && valid && P.film.sum != nullptr;
     FilmAcc fa{0.f, 0.f, 0.f, 0.f};
     if (film) film_load(P.film, HW, p, fa);
-    bool ok = true;
-    for (int c = 0; c < nchunks; c++) {
-        const int sidx = c % kStages;
-        if (!mbar_wait(&full[sidx], (c / kStages) & 1)) {
-            ok = false;
-            break;
-        }
-        const float *stage = stages + (size_t)sidx * stage_floats;
-        const int jn = min(kSB, cnt - c * kSB);
-        for (int j = 0; j < jn; j++) {
-            const float *row = stage + (size_t)j * NCH * kPx + lane;
-            float cur[NL];
-#pragma unroll
-            for (int q = 0; q < NL; q++) cur[q] = row[q * kPx];
-            const uint32_t nn = n0 + (uint32_t)(c * kSB + j) + 1u;
-            if (film) film_add(P.film, p, cur[0], cur[1], cur[2], row[3 * kPx], row[4 * kPx], fa);
-            float rn;
-            switch (kind) {
-                case STATER_TK_LOG1P:
-                    acc_update<float, true, MAXMOM, STATER_TK_LOG1P>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
-                    break;
-                case STATER_TK_SQRT:
-                    acc_update<float, true, MAXMOM, STATER_TK_SQRT>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
-                    break;
-                case STATER_TK_CBRT:
-                    acc_update<float, true, MAXMOM, STATER_TK_CBRT>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
-                    break;
-                case STATER_TK_ASINH:
-                    acc_update<float, true, MAXMOM, STATER_TK_ASINH>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
-                    break;
-                case STATER_TK_BOXCOX:
-                    acc_update<float, true, MAXMOM, STATER_TK_BOXCOX>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
-                    break;
-                default:
-                    acc_update<float, true, MAXMOM, STATER_TK_IDENTITY>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1,
-                                                                         rn);
-            }
-#pragma unroll
-            for (int jf = 0; jf < MAXF; jf++) {
-                const int g = k + jf * P.K;
-                if (g < P.G) feat_update<float, true>(row[(5 + g) * kPx], nn, rn, fm[jf]);
-            }
-        }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[sidx]);
+    bool ok;
+    switch (kind) {
+#define STATER_TMA_CASE(KD)                                                                                      \
+    case KD:                                                                                                     \
+        ok = tma_consume<MAXMOM, MAXF, KD>(P, stages, stage_floats, full, empty, nchunks, cnt, n0, k, lane, p, lam, \
+                                           mean, m2, m3, m4, cx, cy, m1, fm, film, fa);                            \
+        break;
+        STATER_TMA_CASE(STATER_TK_LOG1P)
+        STATER_TMA_CASE(STATER_TK_SQRT)
+        STATER_TMA_CASE(STATER_TK_CBRT)
+        STATER_TMA_CASE(STATER_TK_ASINH)
+        STATER_TMA_CASE(STATER_TK_BOXCOX)
+        default:
+            ok = tma_consume<MAXMOM, MAXF, STATER_TK_IDENTITY>(P, stages, stage_floats, full, empty, nchunks, cnt, n0,
+                                                               k, lane, p, lam, mean, m2, m3, m4, cx, cy, m1, fm,
+                                                               film, fa);
+#undef STATER_TMA_CASE
     }
     if (!ok) {
         if (lane == 0) atomicExch(TP.err, kErrTimeout);
