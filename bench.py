@@ -398,10 +398,16 @@ def run_gpu(args, rank, world, dist):
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         smp = strip_samples(args.cpu_rows, seed=1)
-        v, secs = cpu_pipeline_mpix(smp, threads)
+        # repeat the strip until about 10 s of CPU work have been timed
+        secs, reps = 0.0, 0
+        while secs < 10.0 and reps < 64:
+            _, dt = cpu_pipeline_mpix(smp, threads)
+            secs += dt
+            reps += 1
+        v = reps * 1920 * args.cpu_rows / secs / 1e6
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"1920x{args.cpu_rows} strip of the workload, {secs:.1f} s (FP32 StatTile port + FP64 "
-                         f"denoise restatement)"}
+               "sample": f"{reps} x a 1920x{args.cpu_rows} strip of the workload, {secs:.1f} s (FP32 StatTile "
+                         f"port + film + FP64 denoise restatement)"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,

@@ -1,10 +1,12 @@
 // Stage 2, FP32 form. Same formulas as the plain FP64 form (denoise.cu), laid
 // out for the GPU:
 //  * per-pixel statistics (lnS2, se2, s2, s2C, jb) in one elementwise pass;
-//  * each windowed filter works on a 16 x TY output tile whose (16+2R) x (TY+2R)
-//    halo of every needed plane is staged in shared memory once per transform,
-//    so each HBM byte is read once per tile and every neighbour access is an
-//    on-chip load;
+//  * the windowed filters stream the halo rows of a 32 x TY output tile through
+//    a shared-memory ring holding every transform's planes, so the range weight
+//    of a neighbour is computed once for all transforms (row-ring kernels, up to
+//    5 transforms and 7 feature channels); other configurations, and calls that
+//    ask for the decision bits, use per-transform kernels that stage the whole
+//    (32+2R) x (TY+2R) halo of one transform at a time. Both give the same bits;
 //  * the Welch decisions of all transforms are combined in a per-pixel bit mask
 //    in shared memory (one bit per window position), so the film pass touches
 //    only accepted neighbours;
@@ -609,6 +611,361 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P)
 }
 
 // ---------------------------------------------------------------------------
+// Row-ring forms: every transform per neighbour, one range weight.
+//
+// The halo rows of a 32 x TY tile stream through a ring of TY + 1 shared-memory
+// rows. A ring row holds, as float4 fields in structure-of-arrays order (lane
+// l reads column l: conflict-free 128-bit loads), everything the filter reads
+// at that row: the scaled features and the validity of the pixel, and for every
+// transform the planes of its test and its weighted sums. At window row dy the
+// TY thread rows read the consecutive halo rows dy .. dy + TY - 1 while the CTA
+// loads halo row dy + TY into the one free slot: one barrier per window row.
+// The range weight of a neighbour is computed once and applied to every
+// transform (the per-transform accumulators live in registers), and the
+// operations and their order per transform are those of the per-transform
+// kernels above, so both give the same bits.
+// Features: up to kRingMF channels, validity (or n) in field kRingMF.
+// ---------------------------------------------------------------------------
+constexpr int kRingMF = 7;
+constexpr int kRingFW = 2;  // float4 fields of features + validity
+
+__device__ __forceinline__ float4 f4(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+
+// Feature fields of one halo pixel: scaled features, then `last` in field 7.
+__device__ __forceinline__ void ring_feat_fields(const FeatSet &fs, bool inb, size_t g, float last, float4 &a,
+                                                 float4 &b) {
+    float v[8];
+#pragma unroll
+    for (int f = 0; f < kRingMF; f++) v[f] = (inb && f < fs.nch) ? __ldg(fs.plane[f] + g) * fs.mul[f] : 0.f;
+    v[7] = last;
+    a = f4(v[0], v[1], v[2], v[3]);
+    b = f4(v[4], v[5], v[6], v[7]);
+}
+
+// Vars ring fields per transform k: {lnS2 x3, z^2 se2 (ZPIX) | c0}, {s2 x3, 0 | c1},
+// [{s2C x3, 0 | c2}] with c = z^2 se2 per channel when it depends on it.
+template <bool LEVC, bool ZPIX>
+struct VarsRing {
+    static constexpr int TW = (LEVC || !ZPIX) ? 3 : 2;
+};
+
+template <bool LEVC, bool ZPIX>
+__device__ void vars_ring_load(const FastVars &P, float4 *ring, int slot, int hrow, int x0, int y0, int hw,
+                               int nrec) {
+    constexpr int TW = VarsRing<LEVC, ZPIX>::TW;
+    const size_t HW = (size_t)P.W * P.H;
+    const int gy = y0 - P.R + hrow;
+    for (int idx = threadIdx.x; idx < nrec * hw; idx += blockDim.x) {
+        const int rec = idx / hw, col = idx - rec * hw;
+        const int gx = x0 - P.R + col;
+        const bool inb = gx >= 0 && gx < P.W && gy >= 0 && gy < P.H;
+        const size_t g = inb ? (size_t)gy * P.W + gx : 0;
+        float4 v = f4(0.f, 0.f, 0.f, 0.f);
+        if (rec < kRingFW) {
+            float4 a, b;
+            const float pen = (inb && __ldg(P.n + g) >= 2) ? 0.f : -INFINITY;
+            ring_feat_fields(P.feat, inb, g, pen, a, b);
+            v = rec == 0 ? a : b;
+        } else if (inb) {
+            const int kr = rec - kRingFW, k = kr / TW, sub = kr - k * TW;
+            const float *src = sub == 0 ? P.lnS2[k] : (sub == 1 ? P.s2 + (size_t)k * 3 * HW : P.s2c + (size_t)k * 3 * HW);
+            const bool zero = sub == 2 && !LEVC;
+            v.x = zero ? 0.f : __ldg(src + g);
+            v.y = zero ? 0.f : __ldg(src + HW + g);
+            v.z = zero ? 0.f : __ldg(src + 2 * HW + g);
+            if (ZPIX)
+                v.w = sub == 0 ? __ldg(P.se2[0] + g) * P.z2 : 0.f;
+            else
+                v.w = __ldg(P.se2[k] + (size_t)sub * HW + g) * P.z2;
+        }
+        ring[((size_t)slot * nrec + rec) * hw + col] = v;
+    }
+}
+
+template <bool LEVC, bool ZPIX, int KMAX, int TY>
+__global__ void __launch_bounds__(kTX2 *TY) vars_ring_f32(FastVars P) {
+    constexpr int TW = VarsRing<LEVC, ZPIX>::TW;
+    constexpr int NS = TY + 1;
+    extern __shared__ float4 ring[];
+    const int R = P.R, hw = kTX2 + 2 * R, hh = TY + 2 * R;
+    const int K = P.K, nf = P.feat.nch;
+    const int nrec = kRingFW + K * TW;
+    const int x0 = blockIdx.x * kTX2, y0 = blockIdx.y * TY;
+    const int lx = threadIdx.x % kTX2, tr = threadIdx.x / kTX2;
+    const int x = x0 + lx, y = y0 + tr;
+    const bool in = x < P.W && y < P.H;
+    const size_t HW = (size_t)P.W * P.H;
+    const size_t gi = in ? (size_t)y * P.W + x : 0;
+
+    for (int hrow = 0; hrow < TY; hrow++) vars_ring_load<LEVC, ZPIX>(P, ring, hrow % NS, hrow, x0, y0, hw, nrec);
+
+    // centre values, read as the per-transform kernel stages them
+    const bool vi = in && __ldg(P.n + gi) >= 2;
+    float fi[kRingMF];
+#pragma unroll
+    for (int f = 0; f < kRingMF; f++) fi[f] = (in && f < nf) ? __ldg(P.feat.plane[f] + gi) * P.feat.mul[f] : 0.f;
+    float li[KMAX][3], zi[KMAX][3], aw[KMAX][3], av[KMAX][3], avc[KMAX][3];
+    const float zp = (ZPIX && in) ? __ldg(P.se2[0] + gi) * P.z2 : 0.f;
+#pragma unroll
+    for (int k = 0; k < KMAX; k++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const bool ok = in && k < K;
+            li[k][c] = ok ? __ldg(P.lnS2[k] + (size_t)c * HW + gi) : 0.f;
+            zi[k][c] = ZPIX ? zp : (ok ? __ldg(P.se2[k] + (size_t)c * HW + gi) * P.z2 : 0.f);
+            aw[k][c] = av[k][c] = avc[k][c] = 0.f;
+        }
+    __syncthreads();
+
+    for (int r = -R; r <= R; r++) {
+        const int next = R + r + TY;
+        if (next < hh) vars_ring_load<LEVC, ZPIX>(P, ring, next % NS, next, x0, y0, hw, nrec);
+        if (vi) {
+            const float4 *rp = ring + (size_t)((tr + R + r) % NS) * nrec * hw + lx + R;
+            const float spq = P.ds2 * (float)(r * r);
+#pragma unroll 2
+            for (int dx = -R; dx <= R; dx++) {
+                const float4 F0 = rp[dx], F1 = rp[hw + dx];
+                const float fj[kRingMF] = {F0.x, F0.y, F0.z, F0.w, F1.x, F1.y, F1.z};
+                const float dxs = fmaf(P.ds2, (float)(dx * dx), F1.w);
+                float e = spq + dxs;
+#pragma unroll
+                for (int f = 0; f < kRingMF; f++) {
+                    if (f < nf) {
+                        const float d = fi[f] - fj[f];
+                        e = fmaf(-d, d, e);
+                    }
+                }
+                const float w = fast_exp2(e);
+#pragma unroll
+                for (int k = 0; k < KMAX; k++) {
+                    if (k >= K) break;
+                    const float4 *tp = rp + (size_t)(kRingFW + k * TW) * hw + dx;
+                    const float4 T0 = tp[0], T1 = tp[hw];
+                    const float4 T2 = TW == 3 ? tp[2 * hw] : f4(0.f, 0.f, 0.f, 0.f);
+                    const float lj[3] = {T0.x, T0.y, T0.z}, vj[3] = {T1.x, T1.y, T1.z}, vcj[3] = {T2.x, T2.y, T2.z};
+                    const float zj[3] = {T0.w, T1.w, T2.w};
+                    const float zz = zi[k][0] + T0.w;
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float dl = li[k][c] - lj[c];
+                        const float t = fmaf(-dl, dl, ZPIX ? zz : zi[k][c] + zj[c]);
+                        const float m = t >= 0.f ? w : 0.f;
+                        aw[k][c] += m;
+                        av[k][c] = fmaf(m, vj[c], av[k][c]);
+                        if (LEVC) avc[k][c] = fmaf(m, vcj[c], avc[k][c]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!in) return;
+#pragma unroll
+    for (int k = 0; k < KMAX; k++) {
+        if (k >= K) break;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const float vd = vi ? av[k][c] / aw[k][c] : 0.f;
+            P.varD[k][(size_t)c * HW + gi] = vd;
+            P.varCD[k][(size_t)c * HW + gi] = vi ? (LEVC ? avc[k][c] / aw[k][c] : vd) : 0.f;
+        }
+    }
+}
+
+// Film ring fields: features with n (as float) in field 7, {film x3, 0}, and per
+// transform {mean x3, discr_0}, {discr_1, discr_2, 0, 0}.
+__device__ void film_ring_load(const FastFilm &P, float4 *ring, int slot, int hrow, int x0, int y0, int hw,
+                               int nrec) {
+    const size_t HW = (size_t)P.W * P.H;
+    const int gy = y0 - P.R + hrow;
+    for (int idx = threadIdx.x; idx < nrec * hw; idx += blockDim.x) {
+        const int rec = idx / hw, col = idx - rec * hw;
+        const int gx = x0 - P.R + col;
+        const bool inb = gx >= 0 && gx < P.W && gy >= 0 && gy < P.H;
+        const size_t g = inb ? (size_t)gy * P.W + gx : 0;
+        float4 v = f4(0.f, 0.f, 0.f, 0.f);
+        if (rec < kRingFW) {
+            float4 a, b;
+            int nv = inb ? __ldg(P.n + g) : 0;
+            if (nv < 2) nv = 0;
+            ring_feat_fields(P.feat, inb, g, (float)nv, a, b);
+            v = rec == 0 ? a : b;
+        } else if (inb) {
+            const int kr = rec - kRingFW;
+            if (kr == 0) {
+                v = f4(__ldg(P.film + g), __ldg(P.film + HW + g), __ldg(P.film + 2 * HW + g), 0.f);
+            } else {
+                const int k = (kr - 1) >> 1, sub = (kr - 1) & 1;
+                const float *mean = k == 0 ? P.film : P.mean[k];
+                if (sub == 0)
+                    v = f4(__ldg(mean + g), __ldg(mean + HW + g), __ldg(mean + 2 * HW + g), __ldg(P.discr[k] + g));
+                else
+                    v = f4(__ldg(P.discr[k] + HW + g), __ldg(P.discr[k] + 2 * HW + g), 0.f, 0.f);
+            }
+        }
+        ring[((size_t)slot * nrec + rec) * hw + col] = v;
+    }
+}
+
+template <int KMAX, int TY>
+__global__ void __launch_bounds__(kTX2 *TY) film_ring_f32(FastFilm P) {
+    constexpr int NS = TY + 1;
+    extern __shared__ float4 ring[];
+    __shared__ int s_nmin, s_nmax;
+    const int R = P.R, hw = kTX2 + 2 * R, hh = TY + 2 * R;
+    const int K = P.K, nf = P.feat.nch;
+    const int nrec = kRingFW + 1 + 2 * K;
+    const int x0 = blockIdx.x * kTX2, y0 = blockIdx.y * TY;
+    const int t = threadIdx.x, lx = t % kTX2, tr = t / kTX2;
+    const int x = x0 + lx, y = y0 + tr;
+    const bool in = x < P.W && y < P.H;
+    const size_t HW = (size_t)P.W * P.H;
+    const size_t gi = in ? (size_t)y * P.W + x : 0;
+
+    if (t == 0) {
+        s_nmin = 0x7fffffff;
+        s_nmax = 0;
+    }
+    __syncthreads();
+    {
+        // range of the valid counts in the halo: uniform counts share one pair of df bounds
+        int lmin = 0x7fffffff, lmax = 0;
+        for (int idx = t; idx < hw * hh; idx += blockDim.x) {
+            const int hy = idx / hw, hx = idx - hy * hw;
+            const int gx = x0 - R + hx, gy = y0 - R + hy;
+            if (gx >= 0 && gx < P.W && gy >= 0 && gy < P.H) {
+                const int v = __ldg(P.n + (size_t)gy * P.W + gx);
+                if (v >= 2) {
+                    lmin = min(lmin, v);
+                    lmax = max(lmax, v);
+                }
+            }
+        }
+        atomicMin(&s_nmin, lmin);
+        atomicMax(&s_nmax, lmax);
+    }
+    for (int hrow = 0; hrow < TY; hrow++) film_ring_load(P, ring, hrow % NS, hrow, x0, y0, hw, nrec);
+
+    int ni = in ? __ldg(P.n + gi) : 0;
+    if (ni < 2) ni = 0;
+    const bool act = in && ni >= 2;
+    int ksel = -1;
+    if (act && P.mt_mode == STATER_MT_JB) {
+        ksel = 0;
+        float best = __ldg(P.jb[0] + gi);
+        for (int k = 1; k < K; k++) {
+            const float v = __ldg(P.jb[k] + gi);
+            if (v < best) {
+                best = v;
+                ksel = k;
+            }
+        }
+    }
+    float fi[kRingMF];
+#pragma unroll
+    for (int f = 0; f < kRingMF; f++) fi[f] = (in && f < nf) ? __ldg(P.feat.plane[f] + gi) * P.feat.mul[f] : 0.f;
+    float mi[KMAX][3], di[KMAX][3];
+#pragma unroll
+    for (int k = 0; k < KMAX; k++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const bool ok = in && k < K;
+            const float *mean = k == 0 ? P.film : P.mean[k];
+            mi[k][c] = ok ? __ldg(mean + (size_t)c * HW + gi) : 0.f;
+            di[k][c] = ok ? __ldg(P.discr[k] + (size_t)c * HW + gi) : 0.f;
+        }
+    __syncthreads();
+    const bool uni = s_nmin == s_nmax;
+    float tlo_u = 0.f, thi_u = 0.f;
+    if (uni) {
+        const int dfl = 2 * s_nmin - 2, dfh = s_nmin - 1;
+        tlo_u = dfl > kDfMax ? P.z2lo : __ldg(P.tlo + dfl);
+        thi_u = __ldg(P.thi + (dfh > kDfMax ? kDfMax : dfh));
+    }
+
+    float sw = 0.f, sf[3] = {0.f, 0.f, 0.f};
+    for (int r = -R; r <= R; r++) {
+        const int next = R + r + TY;
+        if (next < hh) film_ring_load(P, ring, next % NS, next, x0, y0, hw, nrec);
+        if (act) {
+            const float4 *rp = ring + (size_t)((tr + R + r) % NS) * nrec * hw + lx + R;
+            const float sdy = P.ds2 * (float)(r * r);
+            for (int dx = -R; dx <= R; dx++) {
+                const float4 F1 = rp[hw + dx];
+                const int nj = (int)F1.w;
+                bool a = nj >= 2;
+                float tlo = tlo_u, thi = thi_u;
+                if (!uni) {
+                    const int njc = max(nj, 2);
+                    const int dfl = ni + njc - 2, dfh = min(ni, njc) - 1;
+                    tlo = dfl > kDfMax ? P.z2lo : __ldg(P.tlo + dfl);
+                    thi = __ldg(P.thi + (dfh > kDfMax ? kDfMax : dfh));
+                }
+#pragma unroll
+                for (int k = 0; k < KMAX; k++) {
+                    if (k >= K) break;
+                    if (!a || (ksel >= 0 && ksel != k)) continue;
+                    const float4 *tp = rp + (size_t)(kRingFW + 1 + 2 * k) * hw + dx;
+                    const float4 T0 = tp[0], T1 = tp[hw];
+                    const float mj[3] = {T0.x, T0.y, T0.z}, dj[3] = {T0.w, T1.x, T1.y};
+                    // qq <= tlo s accepts, qq > thi s rejects, in between the exact df decides
+                    bool acc = true, amb = false;
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float diff = mi[k][c] - mj[c];
+                        const float s = di[k][c] + dj[c];
+                        const float qq = diff * diff;
+                        const bool lo = qq <= tlo * s;
+                        const bool hi = qq <= thi * s;
+                        acc = acc && hi;
+                        amb = amb || (hi && !lo);
+                    }
+                    if (acc && amb) {
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            const float diff = mi[k][c] - mj[c];
+                            const float s = di[k][c] + dj[c];
+                            const float qq = diff * diff;
+                            if (!(qq <= tlo * s) && qq <= thi * s)
+                                acc = acc && welch_exact(diff, di[k][c], dj[c], ni, nj, P.lut, P.lut_n);
+                        }
+                    }
+                    a = acc;
+                }
+                if (dx == 0 && r == 0) a = true;
+                if (a) {
+                    const float4 F0 = rp[dx];
+                    const float fj[kRingMF] = {F0.x, F0.y, F0.z, F0.w, F1.x, F1.y, F1.z};
+                    float e = fmaf(P.ds2, (float)(dx * dx), sdy);
+#pragma unroll
+                    for (int f = 0; f < kRingMF; f++) {
+                        if (f < nf) {
+                            const float d = fi[f] - fj[f];
+                            e = fmaf(-d, d, e);
+                        }
+                    }
+                    const float wt = fast_exp2(e);
+                    const float4 Fm = rp[(size_t)kRingFW * hw + dx];
+                    sw += wt;
+                    sf[0] = fmaf(wt, Fm.x, sf[0]);
+                    sf[1] = fmaf(wt, Fm.y, sf[1]);
+                    sf[2] = fmaf(wt, Fm.z, sf[2]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!in) return;
+    if (!act) {
+        for (int c = 0; c < 3; c++) P.filmD[(size_t)c * HW + gi] = __ldg(P.film + (size_t)c * HW + gi);
+        return;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) P.filmD[(size_t)c * HW + gi] = sf[c] / sw;
+}
+
+// ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
 struct DfTables {
@@ -675,6 +1032,20 @@ constexpr size_t kSmemLimit = 227 * 1024;
 
 int mf_bucket(int nf) { return nf == 0 ? 0 : nf <= 4 ? 4 : nf <= 8 ? 8 : nf <= 16 ? 16 : 24; }
 
+// Row-ring kernels: up to 5 transforms and kRingMF feature channels; TY = 8
+// output rows per tile when the ring fits two CTAs per SM, else TY = 4.
+constexpr size_t kRingSmemMax = 113 * 1024;
+
+int ring_kmax(int K) { return K <= 1 ? 1 : K <= 3 ? 3 : K <= 5 ? 5 : 0; }
+
+size_t ring_smem(int R, int nrec, int TY) { return (size_t)(TY + 1) * nrec * (kTX2 + 2 * R) * sizeof(float4); }
+
+int ring_ty(int R, int nrec) {
+    if (ring_smem(R, nrec, 8) <= kRingSmemMax) return 8;
+    if (ring_smem(R, nrec, 4) <= kRingSmemMax) return 4;
+    return 0;
+}
+
 template <typename KernelT>
 cudaError_t set_smem(KernelT kern, size_t bytes) {
     return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -721,6 +1092,34 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
     STATER_CHECK_LAUNCH("vars_stats_f32");
 
     const bool zp = P.max_moment < 4;
+    {
+        const int km = ring_kmax(P.K);
+        const int nrec = kRingFW + P.K * ((P.levc || !zp) ? 3 : 2);
+        const int ty = ring_ty(P.R, nrec);
+        if (km > 0 && ty > 0 && P.feat.nch <= kRingMF) {
+            const size_t sm = ring_smem(P.R, nrec, ty);
+            dim3 grid((P.W + kTX2 - 1) / kTX2, (P.H + ty - 1) / ty);
+            cudaError_t e = cudaErrorInvalidValue;
+#define STATER_RING_VARS(LV, ZV, KV, TV)                                                   \
+    if ((P.levc != 0) == LV && zp == ZV && km == KV && ty == TV) {                          \
+        e = set_smem(vars_ring_f32<LV, ZV, KV, TV>, sm);                                    \
+        if (e == cudaSuccess) vars_ring_f32<LV, ZV, KV, TV><<<grid, kTX2 * TV, sm, s>>>(P); \
+    }
+#define STATER_RING_VARS_K(LV, ZV, TV) \
+    STATER_RING_VARS(LV, ZV, 1, TV) STATER_RING_VARS(LV, ZV, 3, TV) STATER_RING_VARS(LV, ZV, 5, TV)
+#define STATER_RING_VARS_T(TV)                                                                   \
+    STATER_RING_VARS_K(true, true, TV) STATER_RING_VARS_K(true, false, TV)                        \
+    STATER_RING_VARS_K(false, true, TV) STATER_RING_VARS_K(false, false, TV)
+            STATER_RING_VARS_T(8)
+            STATER_RING_VARS_T(4)
+#undef STATER_RING_VARS_T
+#undef STATER_RING_VARS_K
+#undef STATER_RING_VARS
+            if (e != cudaSuccess) return cuda_status(e, "vars_ring_f32 smem attribute");
+            STATER_CHECK_LAUNCH("vars_ring_f32");
+            return STATER_OK;
+        }
+    }
     int cfg = 0;
     while (cfg < 3 && vars_smem(P.R, P.feat.nch, P.levc != 0, zp, kTileCfg[cfg][0], kTileCfg[cfg][1]) > kSmemLimit) cfg++;
     if (cfg == 3) return set_error(STATER_ERR_UNSUPPORTED, "stater_denoise_vars: radius too large for FP32 tiles");
@@ -786,6 +1185,27 @@ stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s
     film_discr_f32<<<g1, 128, 0, s>>>(P);
     STATER_CHECK_LAUNCH("film_discr_f32");
 
+    {
+        const int km = ring_kmax(P.K);
+        const int nrec = kRingFW + 1 + 2 * P.K;
+        const int ty = ring_ty(P.R, nrec);
+        if (km > 0 && ty > 0 && P.feat.nch <= kRingMF && !P.bits) {
+            const size_t sm = ring_smem(P.R, nrec, ty);
+            dim3 grid((P.W + kTX2 - 1) / kTX2, (P.H + ty - 1) / ty);
+            cudaError_t e = cudaErrorInvalidValue;
+#define STATER_RING_FILM(KV, TV)                                                   \
+    if (km == KV && ty == TV) {                                                     \
+        e = set_smem(film_ring_f32<KV, TV>, sm);                                    \
+        if (e == cudaSuccess) film_ring_f32<KV, TV><<<grid, kTX2 * TV, sm, s>>>(P); \
+    }
+            STATER_RING_FILM(1, 8) STATER_RING_FILM(3, 8) STATER_RING_FILM(5, 8)
+            STATER_RING_FILM(1, 4) STATER_RING_FILM(3, 4) STATER_RING_FILM(5, 4)
+#undef STATER_RING_FILM
+            if (e != cudaSuccess) return cuda_status(e, "film_ring_f32 smem attribute");
+            STATER_CHECK_LAUNCH("film_ring_f32");
+            return STATER_OK;
+        }
+    }
     int cfg = 0;
     while (cfg < 3 && film_smem(P.R, P.feat.nch, kTileCfg[cfg][0], kTileCfg[cfg][1]) > kSmemLimit) cfg++;
     if (cfg == 3) return set_error(STATER_ERR_UNSUPPORTED, "stater_denoise_film: radius too large for FP32 tiles");

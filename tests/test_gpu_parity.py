@@ -329,3 +329,24 @@ def test_lev_matches_oracle(st):
         r2 = host(lev.r2).astype(np.float64)
         assert np.max(np.abs(r2 - ref["r2"])) <= tol
     assert 0.4 < float(np.median(ref["r2"])) < 0.8
+
+
+@pytest.mark.parametrize("W,H,tr,mm,R,mt_mode", [
+    (160, 96, BASE_TR, 3, 10, 2),
+    (97, 61, BASE_TR[:3], 5, 7, 3),
+    (64, 48, BASE_TR[:1], 4, 20, 2),
+])
+def test_fp32_film_filter_forms_agree(st, W, H, tr, mm, R, mt_mode):
+    """The row-ring film filter (all transforms per neighbour) and the
+    per-transform filter that also writes the decision bits give the same filmD."""
+    s = synth_samples(W, H, 48, G=7, seed=21, region=2)
+    b = st.StatBuffers(W, H, tr, 7, mm, st.F32)
+    b.accumulate(dev(s), mode=st.ACC_FAST)
+    specs = [st.GBufferSpec(a, c, sg) for a, c, sg in GSPEC]
+    b.denoise_vars(radius=R, gbuffers=specs)
+    b.denoise_film(radius=R, gbuffers=specs, mt_mode=mt_mode)
+    ring = b.filmD.clone()
+    bits = torch.zeros(H * W, len(tr), st.bits_words(R), dtype=torch.int32, device="cuda")
+    b.denoise_film(radius=R, gbuffers=specs, mt_mode=mt_mode, accept_bits=bits)
+    torch.cuda.synchronize()
+    assert torch.equal(ring, b.filmD)
