@@ -650,35 +650,64 @@ struct VarsRing {
 };
 
 template <bool LEVC, bool ZPIX>
-__device__ void vars_ring_load(const FastVars &P, float4 *ring, int slot, int hrow, int x0, int y0, int hw,
-                               int nrec) {
+__device__ __forceinline__ float4 vars_ring_value(const FastVars &P, int rec, int col, int hrow, int x0, int y0) {
     constexpr int TW = VarsRing<LEVC, ZPIX>::TW;
     const size_t HW = (size_t)P.W * P.H;
-    const int gy = y0 - P.R + hrow;
+    const int gy = y0 - P.R + hrow, gx = x0 - P.R + col;
+    const bool inb = gx >= 0 && gx < P.W && gy >= 0 && gy < P.H;
+    const size_t g = inb ? (size_t)gy * P.W + gx : 0;
+    float4 v = f4(0.f, 0.f, 0.f, 0.f);
+    if (rec < kRingFW) {
+        float4 a, b;
+        const float pen = (inb && __ldg(P.n + g) >= 2) ? 0.f : -INFINITY;
+        ring_feat_fields(P.feat, inb, g, pen, a, b);
+        v = rec == 0 ? a : b;
+    } else if (inb) {
+        const int kr = rec - kRingFW, k = kr / TW, sub = kr - k * TW;
+        const float *src = sub == 0 ? P.lnS2[k] : (sub == 1 ? P.s2 + (size_t)k * 3 * HW : P.s2c + (size_t)k * 3 * HW);
+        const bool zero = sub == 2 && !LEVC;
+        v.x = zero ? 0.f : __ldg(src + g);
+        v.y = zero ? 0.f : __ldg(src + HW + g);
+        v.z = zero ? 0.f : __ldg(src + 2 * HW + g);
+        if (ZPIX)
+            v.w = sub == 0 ? __ldg(P.se2[0] + g) * P.z2 : 0.f;
+        else
+            v.w = __ldg(P.se2[k] + (size_t)sub * HW + g) * P.z2;
+    }
+    return v;
+}
+
+// Ring row loaders. A CTA loads one halo row of nrec x hw fields; with the
+// pipelined form each thread fetches its (at most kRingPer) fields into
+// registers before the window row's arithmetic and stores them after it, so
+// the loads' latency is hidden behind the arithmetic.
+constexpr int kRingPer = 5;
+
+template <typename ValueFn>
+__device__ __forceinline__ void ring_load_now(float4 *ring, int slot, int hrow, int hw, int nrec, ValueFn value) {
     for (int idx = threadIdx.x; idx < nrec * hw; idx += blockDim.x) {
         const int rec = idx / hw, col = idx - rec * hw;
-        const int gx = x0 - P.R + col;
-        const bool inb = gx >= 0 && gx < P.W && gy >= 0 && gy < P.H;
-        const size_t g = inb ? (size_t)gy * P.W + gx : 0;
-        float4 v = f4(0.f, 0.f, 0.f, 0.f);
-        if (rec < kRingFW) {
-            float4 a, b;
-            const float pen = (inb && __ldg(P.n + g) >= 2) ? 0.f : -INFINITY;
-            ring_feat_fields(P.feat, inb, g, pen, a, b);
-            v = rec == 0 ? a : b;
-        } else if (inb) {
-            const int kr = rec - kRingFW, k = kr / TW, sub = kr - k * TW;
-            const float *src = sub == 0 ? P.lnS2[k] : (sub == 1 ? P.s2 + (size_t)k * 3 * HW : P.s2c + (size_t)k * 3 * HW);
-            const bool zero = sub == 2 && !LEVC;
-            v.x = zero ? 0.f : __ldg(src + g);
-            v.y = zero ? 0.f : __ldg(src + HW + g);
-            v.z = zero ? 0.f : __ldg(src + 2 * HW + g);
-            if (ZPIX)
-                v.w = sub == 0 ? __ldg(P.se2[0] + g) * P.z2 : 0.f;
-            else
-                v.w = __ldg(P.se2[k] + (size_t)sub * HW + g) * P.z2;
+        ring[((size_t)slot * nrec + rec) * hw + col] = value(rec, col, hrow);
+    }
+}
+
+template <typename ValueFn>
+__device__ __forceinline__ void ring_fetch(float4 (&pend)[kRingPer], int hrow, int hw, int nrec, ValueFn value) {
+#pragma unroll
+    for (int i = 0; i < kRingPer; i++) {
+        const int idx = threadIdx.x + i * blockDim.x;
+        if (idx < nrec * hw) {
+            const int rec = idx / hw;
+            pend[i] = value(rec, idx - rec * hw, hrow);
         }
-        ring[((size_t)slot * nrec + rec) * hw + col] = v;
+    }
+}
+
+__device__ __forceinline__ void ring_store(const float4 (&pend)[kRingPer], float4 *ring, int slot, int hw, int nrec) {
+#pragma unroll
+    for (int i = 0; i < kRingPer; i++) {
+        const int idx = threadIdx.x + i * blockDim.x;
+        if (idx < nrec * hw) ring[(size_t)slot * nrec * hw + idx] = pend[i];
     }
 }
 
@@ -697,7 +726,10 @@ __global__ void __launch_bounds__(kTX2 *TY) vars_ring_f32(FastVars P) {
     const size_t HW = (size_t)P.W * P.H;
     const size_t gi = in ? (size_t)y * P.W + x : 0;
 
-    for (int hrow = 0; hrow < TY; hrow++) vars_ring_load<LEVC, ZPIX>(P, ring, hrow % NS, hrow, x0, y0, hw, nrec);
+    // (the variance filter is bound by shared-memory bandwidth, not by the
+    // latency of these loads: they are stored as they arrive)
+    auto value = [&](int rec, int col, int hrow) { return vars_ring_value<LEVC, ZPIX>(P, rec, col, hrow, x0, y0); };
+    for (int hrow = 0; hrow < TY; hrow++) ring_load_now(ring, hrow % NS, hrow, hw, nrec, value);
 
     // centre values, read as the per-transform kernel stages them
     const bool vi = in && __ldg(P.n + gi) >= 2;
@@ -719,7 +751,7 @@ __global__ void __launch_bounds__(kTX2 *TY) vars_ring_f32(FastVars P) {
 
     for (int r = -R; r <= R; r++) {
         const int next = R + r + TY;
-        if (next < hh) vars_ring_load<LEVC, ZPIX>(P, ring, next % NS, next, x0, y0, hw, nrec);
+        if (next < hh) ring_load_now(ring, next % NS, next, hw, nrec, value);
         if (vi) {
             const float4 *rp = ring + (size_t)((tr + R + r) % NS) * nrec * hw + lx + R;
             const float spq = P.ds2 * (float)(r * r);
@@ -775,41 +807,36 @@ __global__ void __launch_bounds__(kTX2 *TY) vars_ring_f32(FastVars P) {
 
 // Film ring fields: features with n (as float) in field 7, {film x3, 0}, and per
 // transform {mean x3, discr_0}, {discr_1, discr_2, 0, 0}.
-__device__ void film_ring_load(const FastFilm &P, float4 *ring, int slot, int hrow, int x0, int y0, int hw,
-                               int nrec) {
+__device__ __forceinline__ float4 film_ring_value(const FastFilm &P, int rec, int col, int hrow, int x0, int y0) {
     const size_t HW = (size_t)P.W * P.H;
-    const int gy = y0 - P.R + hrow;
-    for (int idx = threadIdx.x; idx < nrec * hw; idx += blockDim.x) {
-        const int rec = idx / hw, col = idx - rec * hw;
-        const int gx = x0 - P.R + col;
-        const bool inb = gx >= 0 && gx < P.W && gy >= 0 && gy < P.H;
-        const size_t g = inb ? (size_t)gy * P.W + gx : 0;
-        float4 v = f4(0.f, 0.f, 0.f, 0.f);
-        if (rec < kRingFW) {
-            float4 a, b;
-            int nv = inb ? __ldg(P.n + g) : 0;
-            if (nv < 2) nv = 0;
-            ring_feat_fields(P.feat, inb, g, (float)nv, a, b);
-            v = rec == 0 ? a : b;
-        } else if (inb) {
-            const int kr = rec - kRingFW;
-            if (kr == 0) {
-                v = f4(__ldg(P.film + g), __ldg(P.film + HW + g), __ldg(P.film + 2 * HW + g), 0.f);
-            } else {
-                const int k = (kr - 1) >> 1, sub = (kr - 1) & 1;
-                const float *mean = k == 0 ? P.film : P.mean[k];
-                if (sub == 0)
-                    v = f4(__ldg(mean + g), __ldg(mean + HW + g), __ldg(mean + 2 * HW + g), __ldg(P.discr[k] + g));
-                else
-                    v = f4(__ldg(P.discr[k] + HW + g), __ldg(P.discr[k] + 2 * HW + g), 0.f, 0.f);
-            }
+    const int gy = y0 - P.R + hrow, gx = x0 - P.R + col;
+    const bool inb = gx >= 0 && gx < P.W && gy >= 0 && gy < P.H;
+    const size_t g = inb ? (size_t)gy * P.W + gx : 0;
+    float4 v = f4(0.f, 0.f, 0.f, 0.f);
+    if (rec < kRingFW) {
+        float4 a, b;
+        int nv = inb ? __ldg(P.n + g) : 0;
+        if (nv < 2) nv = 0;
+        ring_feat_fields(P.feat, inb, g, (float)nv, a, b);
+        v = rec == 0 ? a : b;
+    } else if (inb) {
+        const int kr = rec - kRingFW;
+        if (kr == 0) {
+            v = f4(__ldg(P.film + g), __ldg(P.film + HW + g), __ldg(P.film + 2 * HW + g), 0.f);
+        } else {
+            const int k = (kr - 1) >> 1, sub = (kr - 1) & 1;
+            const float *mean = k == 0 ? P.film : P.mean[k];
+            if (sub == 0)
+                v = f4(__ldg(mean + g), __ldg(mean + HW + g), __ldg(mean + 2 * HW + g), __ldg(P.discr[k] + g));
+            else
+                v = f4(__ldg(P.discr[k] + HW + g), __ldg(P.discr[k] + 2 * HW + g), 0.f, 0.f);
         }
-        ring[((size_t)slot * nrec + rec) * hw + col] = v;
     }
+    return v;
 }
 
 template <int KMAX, int TY>
-__global__ void __launch_bounds__(kTX2 *TY) film_ring_f32(FastFilm P) {
+__global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
     constexpr int NS = TY + 1;
     extern __shared__ float4 ring[];
     __shared__ int s_nmin, s_nmax;
@@ -845,7 +872,10 @@ __global__ void __launch_bounds__(kTX2 *TY) film_ring_f32(FastFilm P) {
         atomicMin(&s_nmin, lmin);
         atomicMax(&s_nmax, lmax);
     }
-    for (int hrow = 0; hrow < TY; hrow++) film_ring_load(P, ring, hrow % NS, hrow, x0, y0, hw, nrec);
+    auto value = [&](int rec, int col, int hrow) { return film_ring_value(P, rec, col, hrow, x0, y0); };
+    const bool pipelined = nrec * hw <= kRingPer * (int)blockDim.x;
+    float4 pend[kRingPer];
+    for (int hrow = 0; hrow < TY; hrow++) ring_load_now(ring, hrow % NS, hrow, hw, nrec, value);
 
     int ni = in ? __ldg(P.n + gi) : 0;
     if (ni < 2) ni = 0;
@@ -887,7 +917,12 @@ __global__ void __launch_bounds__(kTX2 *TY) film_ring_f32(FastFilm P) {
     float sw = 0.f, sf[3] = {0.f, 0.f, 0.f};
     for (int r = -R; r <= R; r++) {
         const int next = R + r + TY;
-        if (next < hh) film_ring_load(P, ring, next % NS, next, x0, y0, hw, nrec);
+        if (next < hh) {
+            if (pipelined)
+                ring_fetch(pend, next, hw, nrec, value);
+            else
+                ring_load_now(ring, next % NS, next, hw, nrec, value);
+        }
         if (act) {
             const float4 *rp = ring + (size_t)((tr + R + r) % NS) * nrec * hw + lx + R;
             const float sdy = P.ds2 * (float)(r * r);
@@ -954,6 +989,7 @@ __global__ void __launch_bounds__(kTX2 *TY) film_ring_f32(FastFilm P) {
                 }
             }
         }
+        if (pipelined && next < hh) ring_store(pend, ring, next % NS, hw, nrec);
         __syncthreads();
     }
     if (!in) return;
