@@ -100,12 +100,13 @@ __device__ __forceinline__ T acc_transform(float lambda, T x) {
     }
 }
 
-// One sample's update of one transform's moments for one channel.
-template <typename T, bool FAST, int MAXMOM>
+// One sample's update of one transform's moments for one channel. PEELED: the
+// caller handles a pixel's first sample separately (acc_first), so nn >= 2.
+template <typename T, bool FAST, int MAXMOM, bool PEELED = false>
 __device__ __forceinline__ void acc_update1(T x, uint32_t nn, T rn, float xD, float yD, T &mean, T &m2, T &m3, T &m4,
                                             T &cx, T &cy, T &m1) {
     const T nT = (T)nn;
-    if (FAST && nn == 1u) {
+    if (FAST && !PEELED && nn == 1u) {
         // First sample: the update reduces to mean = x with every central
         // moment exactly 0. Taking that directly keeps FMA contraction from
         // leaving rounding residue of the size of x^3 in m3 (the EXACT form
@@ -137,7 +138,7 @@ __device__ __forceinline__ void acc_update1(T x, uint32_t nn, T rn, float xD, fl
 
 // One sample's update of one transform's moments (3 channels). `cur` holds
 // R, G, B and, with MAXMOM >= 5, the in-pixel offsets u, v.
-template <typename T, bool FAST, int MAXMOM, int KIND>
+template <typename T, bool FAST, int MAXMOM, int KIND, bool PEELED = false>
 __device__ __forceinline__ void acc_update(const float *cur, uint32_t nn, float lam, T (&mean)[3], T (&m2)[3],
                                            T (&m3)[3], T (&m4)[3], T (&cx)[3], T (&cy)[3], T (&m1)[3], T &rn_out) {
     T rn = T(0);
@@ -157,8 +158,17 @@ __device__ __forceinline__ void acc_update(const float *cur, uint32_t nn, float 
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         const T x = acc_transform<T, FAST, KIND>(lam, (T)cur[c]);
-        acc_update1<T, FAST, MAXMOM>(x, nn, rn, xD, yD, mean[c], m2[c], m3[c], m4[c], cx[c], cy[c], m1[c]);
+        acc_update1<T, FAST, MAXMOM, PEELED>(x, nn, rn, xD, yD, mean[c], m2[c], m3[c], m4[c], cx[c], cy[c], m1[c]);
     }
+}
+
+// FAST form, a pixel's first sample (n becomes 1): the update reduces to
+// mean = x with every central moment 0 (they are 0 already), so the sample
+// loop that follows needs no first-sample test.
+template <int KIND, typename T>
+__device__ __forceinline__ void acc_first(const float *cur, float lam, T (&mean)[3]) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) mean[c] = (T)acc_transform<float, true, KIND>(lam, cur[c]);
 }
 
 // FAST transform chosen at run time (the kind is uniform across a warp).
@@ -212,7 +222,13 @@ __device__ __forceinline__ void acc_loop(const AccParams &P, size_t p, int k, in
             film_add(P.film, p, cur[0], cur[1], cur[2], u, v, fa);
         }
         T rn;
-        acc_update<T, FAST, MAXMOM, KIND>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
+        if (FAST && nn == 1u) {
+            // first sample: mean = x; the feature means take the sample (rn = 1)
+            acc_first<KIND>(cur, lam, mean);
+            rn = T(1);
+        } else {
+            acc_update<T, FAST, MAXMOM, KIND, FAST>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
+        }
 #pragma unroll
         for (int jf = 0; jf < MAXF; jf++) {
             const int g = k + jf * P.K;
@@ -314,6 +330,7 @@ template <typename T, bool FAST, int MAXMOM>
 cudaError_t launch_acc_m(const AccParams &P, cudaStream_t s) {
     const int per = P.G == 0 ? 0 : (P.G + P.K - 1) / P.K;
     if (per == 0) return launch_acc_mf<T, FAST, MAXMOM, 0>(P, s);
+    if (per <= 2) return launch_acc_mf<T, FAST, MAXMOM, 2>(P, s);
     if (per <= 4) return launch_acc_mf<T, FAST, MAXMOM, 4>(P, s);
     if (per <= 8) return launch_acc_mf<T, FAST, MAXMOM, 8>(P, s);
     return launch_acc_mf<T, FAST, MAXMOM, 16>(P, s);

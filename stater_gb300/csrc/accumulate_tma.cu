@@ -98,7 +98,23 @@ __device__ __forceinline__ bool tma_consume(const AccParams &P, const float *sta
         if (!mbar_wait(&full[sidx], (c / kStages) & 1)) return false;
         const float *stage = stages + (size_t)sidx * stage_floats;
         const int jn = min(kSB, cnt - c * kSB);
-        for (int j = 0; j < jn; j++) {
+        int j0 = 0;
+        if (c == 0 && n0 == 0u && jn > 0) {
+            // the pixel's first sample: mean = x, the feature means take the sample
+            const float *row = stage + lane;
+            float cur[NL];
+#pragma unroll
+            for (int q = 0; q < NL; q++) cur[q] = row[q * kPx];
+            if (film) film_add(P.film, p, cur[0], cur[1], cur[2], row[3 * kPx], row[4 * kPx], fa);
+            acc_first<KIND>(cur, lam, mean);
+#pragma unroll
+            for (int jf = 0; jf < MAXF; jf++) {
+                const int g = k + jf * P.K;
+                if (g < P.G) feat_update<float, true>(row[(5 + g) * kPx], 1u, 1.f, fm[jf]);
+            }
+            j0 = 1;
+        }
+        for (int j = j0; j < jn; j++) {
             const float *row = stage + (size_t)j * NCH * kPx + lane;
             float cur[NL];
 #pragma unroll
@@ -106,7 +122,7 @@ __device__ __forceinline__ bool tma_consume(const AccParams &P, const float *sta
             const uint32_t nn = n0 + (uint32_t)(c * kSB + j) + 1u;
             if (film) film_add(P.film, p, cur[0], cur[1], cur[2], row[3 * kPx], row[4 * kPx], fa);
             float rn;
-            acc_update<float, true, MAXMOM, KIND>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
+            acc_update<float, true, MAXMOM, KIND, true>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
 #pragma unroll
             for (int jf = 0; jf < MAXF; jf++) {
                 const int g = k + jf * P.K;
@@ -270,6 +286,7 @@ template <int MAXMOM>
 cudaError_t launch_tma_m(const CUtensorMap &map, const TmaAccParams &TP, cudaStream_t s) {
     const int per = TP.P.G == 0 ? 0 : (TP.P.G + TP.P.K - 1) / TP.P.K;
     if (per == 0) return launch_tma_mf<MAXMOM, 0>(map, TP, s);
+    if (per <= 2) return launch_tma_mf<MAXMOM, 2>(map, TP, s);
     if (per <= 4) return launch_tma_mf<MAXMOM, 4>(map, TP, s);
     if (per <= 8) return launch_tma_mf<MAXMOM, 8>(map, TP, s);
     return launch_tma_mf<MAXMOM, 16>(map, TP, s);
