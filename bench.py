@@ -282,8 +282,9 @@ def run_gpu(args, rank, world, dist):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     # DRAM bytes per launch from one ncu capture of acc_tma_kernel at 480x272, 64 spp
-    # (428.8 MB read + 22.5 MB written), scaled by the pixel-samples of this launch.
-    traffic = (428.825856e6 + 22.54848e6) * (HW * SPP) / (480 * 272 * 64) / 1e9
+    # (431.5 MB read + 27.0 MB written, film sums included), scaled by the
+    # pixel-samples of this launch.
+    traffic = (431.457536e6 + 26.955776e6) * (HW * SPP) / (480 * 272 * 64) / 1e9
     roofline = {"kernel": "acc_tma_kernel (stage-1 accumulation)", "bound": "hbm",
                 "achieved": acc_bytes / (acc_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                 "frac": acc_bytes / (acc_ms / 1e3) / 1e9 / hbm_peak, "traffic": traffic,
