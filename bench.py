@@ -199,6 +199,16 @@ def _reset(b, film):
     film.clear()
 
 
+def max_over_ranks(ms, world, dist, device="cuda"):
+    """The largest of the ranks' timings: the job is as slow as its slowest replica."""
+    import torch
+    if world <= 1 or dist is None:
+        return float(ms)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_gpu(args, rank, world, dist):
     import numpy as np
     import torch
@@ -264,11 +274,7 @@ def run_gpu(args, rank, world, dist):
     if world > 1:
         dist.barrier()
     per_step = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
-    total_ms = evs[0].elapsed_time(evs[steps])
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(evs[0].elapsed_time(evs[steps]), world, dist)
     value = world * HW * steps / (total_ms / 1e3) / 1e6
     filmD_check = float(b.filmD.double().mean().item())
 
@@ -386,11 +392,7 @@ def run_gpu(args, rank, world, dist):
         e1.record(stream)
         torch.cuda.synchronize()
         e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
-        e2e_val = HW / (e2e_ms / 1e3) / 1e6
-        if world > 1:
-            t = torch.tensor([e2e_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_val = world * HW / (float(t.item()) / 1e3) / 1e6
+        e2e_val = world * HW / (max_over_ranks(e2e_ms, world, dist) / 1e3) / 1e6
         e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": SPP * (5 + G) * HW * 4,
                "d2h_bytes_per_step": 3 * HW * 4, "ms_per_step": e2e_ms,
                "path": "pinned host samples -> 32-spp chunks (copy stream) -> accumulate + film sums -> film image "
