@@ -33,13 +33,57 @@ struct AccParams {
     // Optional film sums (film.sum == nullptr: off), added by the transform-0
     // threads from the samples they read anyway.
     FilmTarget film;
+    // Feature channels whose running means transform k's threads keep
+    // (featmap[k][j] < 0: none); chosen on the host so that the cheap
+    // transforms' threads carry them (acc_assign_features).
+    int8_t featmap[STATER_MAX_TRANSFORMS][STATER_MAX_FEATURES];
+    int maxf;  // largest number of channels one transform keeps
 };
+
+// Relative cost of one sample's update per transform kind (FAST form), used
+// to hand the feature channels to the threads with the cheapest transforms.
+inline float acc_kind_cost(int kind) {
+    switch (kind) {
+        case STATER_TK_IDENTITY: return 1.0f;
+        case STATER_TK_SQRT: return 1.15f;
+        case STATER_TK_LOG1P: return 1.5f;
+        case STATER_TK_CBRT: return 1.5f;
+        case STATER_TK_ASINH: return 1.5f;
+        default: return 1.8f;
+    }
+}
+
+// Assigns the G feature channels to transforms (greedily to the cheapest
+// current load; transform 0 also carries the film). Returns the largest
+// number of channels one transform keeps.
+inline int acc_assign_features(AccParams &P) {
+    float load[STATER_MAX_TRANSFORMS];
+    int cnt[STATER_MAX_TRANSFORMS];
+    for (int k = 0; k < STATER_MAX_TRANSFORMS; k++) {
+        load[k] = k < P.K ? acc_kind_cost(P.ts.kind[k]) + (k == 0 && P.film.sum ? 0.2f : 0.f) : 1e30f;
+        cnt[k] = 0;
+        for (int j = 0; j < STATER_MAX_FEATURES; j++) P.featmap[k][j] = -1;
+    }
+    int maxc = 0;
+    for (int g = 0; g < P.G; g++) {
+        int best = 0;
+        for (int k = 1; k < P.K; k++)
+            if (load[k] < load[best]) best = k;
+        P.featmap[best][cnt[best]++] = (int8_t)g;
+        load[best] += 0.15f;
+        if (cnt[best] > maxc) maxc = cnt[best];
+    }
+    return maxc;
+}
 
 // Compact FP32 forms used by the FAST mode (few instructions, no slow paths;
 // accurate to a few 1e-7 relative, checked against the FP64 oracle):
-//   log1p: 2 atanh(t), t = x/(2+x), by its Taylor series t + t^3/3 + ... + t^9/9
-//          for x < 1/4 (t < 1/9), else log2(1+x) ln 2 with the hardware log2;
-//   asinh: log1p(x + x^2/(1 + sqrt(1 + x^2))), odd;
+//   log1p: 2 atanh(t), t = x/(2+x), by its Taylor series t + t^3/3 + t^5/5
+//          for x < 1/4 (t < 1/9; truncation below 4e-7 relative), else
+//          log2(1+x) ln 2 with the hardware log2;
+//   asinh: for |x| < 1/4 its Taylor series x - x^3/6 + 3x^5/40 - 5x^7/112
+//          (truncation below 5e-7 relative), else log2(|x| + sqrt(x^2 + 1)) ln 2
+//          (2|x| above 1e18, where x^2 would overflow), odd;
 //   cbrt:  2^(log2|x| / 3) refined by one Newton step, odd;
 //   sqrt:  x * rsqrt(x).
 __device__ __forceinline__ float fast_log2(float x) {
@@ -55,9 +99,7 @@ __device__ __forceinline__ float fast_exp2(float x) {
 __device__ __forceinline__ float log1p_compact(float x) {
     const float t = __fdividef(x, 2.f + x);
     const float t2 = t * t;
-    float p = fmaf(t2, 1.f / 9.f, 1.f / 7.f);
-    p = fmaf(t2, p, 1.f / 5.f);
-    p = fmaf(t2, p, 1.f / 3.f);
+    float p = fmaf(t2, 1.f / 5.f, 1.f / 3.f);
     p = fmaf(t2, p, 1.f);
     const float small = 2.f * t * p;
     const float large = fast_log2(1.f + x) * 0.69314718055994531f;
@@ -65,10 +107,15 @@ __device__ __forceinline__ float log1p_compact(float x) {
 }
 __device__ __forceinline__ float asinh_compact(float x) {
     const float a = fabsf(x);
+    const float a2 = a * a;
+    float p = fmaf(a2, -5.f / 112.f, 3.f / 40.f);
+    p = fmaf(a2, p, -1.f / 6.f);
+    p = fmaf(a2, p, 1.f);
+    const float small = a * p;
     const float v = fmaf(a, a, 1.f);
-    const float sq = v * rsqrtf(v);
-    const float r = log1p_compact(a + __fdividef(a * a, 1.f + sq));
-    return copysignf(r, x);
+    const float t = a > 1e18f ? 2.f * a : a + v * rsqrtf(v);
+    const float large = fast_log2(t) * 0.69314718055994531f;
+    return copysignf(a < 0.25f ? small : large, x);
 }
 __device__ __forceinline__ float cbrt_compact(float x) {
     const float a = fabsf(x);
@@ -231,8 +278,8 @@ __device__ __forceinline__ void acc_loop(const AccParams &P, size_t p, int k, in
         }
 #pragma unroll
         for (int jf = 0; jf < MAXF; jf++) {
-            const int g = k + jf * P.K;
-            if (g < P.G) feat_update<T, FAST>(__ldg(spc + (size_t)(5 + g) * HW), nn, rn, fm[jf]);
+            const int g = P.featmap[k][jf];
+            if (g >= 0) feat_update<T, FAST>(__ldg(spc + (size_t)(5 + g) * HW), nn, rn, fm[jf]);
         }
     }
 }
@@ -267,8 +314,8 @@ __global__ void __launch_bounds__(256) acc_kernel(AccParams P) {
     T fm[MAXF > 0 ? MAXF : 1];
 #pragma unroll
     for (int j = 0; j < MAXF; j++) {
-        const int g = k + j * P.K;
-        fm[j] = g < P.G ? gm[(size_t)g * HW + p] : T(0);
+        const int g = P.featmap[k][j];
+        fm[j] = g >= 0 ? gm[(size_t)g * HW + p] : T(0);
     }
     const float lam = P.ts.lambda[k];
     // the film sums ride along with transform 0 (warp-uniform: k = threadIdx.y)
@@ -306,8 +353,8 @@ __global__ void __launch_bounds__(256) acc_kernel(AccParams P) {
     }
 #pragma unroll
     for (int j = 0; j < MAXF; j++) {
-        const int g = k + j * P.K;
-        if (g < P.G) gm[(size_t)g * HW + p] = fm[j];
+        const int g = P.featmap[k][j];
+        if (g >= 0) gm[(size_t)g * HW + p] = fm[j];
     }
     if (k == 0) P.n[p] = (int32_t)(n0 + (uint32_t)cnt);
 }
@@ -328,7 +375,7 @@ cudaError_t launch_acc_mf(const AccParams &P, cudaStream_t s) {
 
 template <typename T, bool FAST, int MAXMOM>
 cudaError_t launch_acc_m(const AccParams &P, cudaStream_t s) {
-    const int per = P.G == 0 ? 0 : (P.G + P.K - 1) / P.K;
+    const int per = P.maxf;
     if (per == 0) return launch_acc_mf<T, FAST, MAXMOM, 0>(P, s);
     if (per <= 2) return launch_acc_mf<T, FAST, MAXMOM, 2>(P, s);
     if (per <= 4) return launch_acc_mf<T, FAST, MAXMOM, 4>(P, s);

@@ -247,6 +247,7 @@ stater_status stater_accumulate(const stater_accumulate_args *a, stater_stream s
     P.film.sum = a->film_contrib_sum;
     P.film.weight = a->film_weight_sum;
     P.film.spill = a->film_spill;
+    P.maxf = acc_assign_features(P);
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e;
     if (a->mode == STATER_ACC_FAST) {

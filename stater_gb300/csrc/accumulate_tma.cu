@@ -109,8 +109,8 @@ __device__ __forceinline__ bool tma_consume(const AccParams &P, const float *sta
             acc_first<KIND>(cur, lam, mean);
 #pragma unroll
             for (int jf = 0; jf < MAXF; jf++) {
-                const int g = k + jf * P.K;
-                if (g < P.G) feat_update<float, true>(row[(5 + g) * kPx], 1u, 1.f, fm[jf]);
+                const int g = P.featmap[k][jf];
+                if (g >= 0) feat_update<float, true>(row[(5 + g) * kPx], 1u, 1.f, fm[jf]);
             }
             j0 = 1;
         }
@@ -125,8 +125,8 @@ __device__ __forceinline__ bool tma_consume(const AccParams &P, const float *sta
             acc_update<float, true, MAXMOM, KIND, true>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
 #pragma unroll
             for (int jf = 0; jf < MAXF; jf++) {
-                const int g = k + jf * P.K;
-                if (g < P.G) feat_update<float, true>(row[(5 + g) * kPx], nn, rn, fm[jf]);
+                const int g = P.featmap[k][jf];
+                if (g >= 0) feat_update<float, true>(row[(5 + g) * kPx], nn, rn, fm[jf]);
             }
         }
         __syncwarp();
@@ -218,8 +218,8 @@ __global__ void __launch_bounds__(kPx *STATER_MAX_TRANSFORMS + 32)
     float fm[MAXF > 0 ? MAXF : 1];
 #pragma unroll
     for (int j = 0; j < MAXF; j++) {
-        const int g = k + j * P.K;
-        fm[j] = (g < P.G && valid) ? gm[(size_t)g * HW + p] : 0.f;
+        const int g = P.featmap[k][j];
+        fm[j] = (g >= 0 && valid) ? gm[(size_t)g * HW + p] : 0.f;
     }
     const int kind = P.ts.kind[k];
     const float lam = P.ts.lambda[k];
@@ -264,8 +264,8 @@ __global__ void __launch_bounds__(kPx *STATER_MAX_TRANSFORMS + 32)
     }
 #pragma unroll
     for (int j = 0; j < MAXF; j++) {
-        const int g = k + j * P.K;
-        if (g < P.G) gm[(size_t)g * HW + p] = fm[j];
+        const int g = P.featmap[k][j];
+        if (g >= 0) gm[(size_t)g * HW + p] = fm[j];
     }
     if (film) film_store(P.film, HW, p, fa);
     if (k == 0) P.n[p] = (int32_t)(n0 + (uint32_t)cnt);
@@ -284,7 +284,7 @@ cudaError_t launch_tma_mf(const CUtensorMap &map, const TmaAccParams &TP, cudaSt
 
 template <int MAXMOM>
 cudaError_t launch_tma_m(const CUtensorMap &map, const TmaAccParams &TP, cudaStream_t s) {
-    const int per = TP.P.G == 0 ? 0 : (TP.P.G + TP.P.K - 1) / TP.P.K;
+    const int per = TP.P.maxf;
     if (per == 0) return launch_tma_mf<MAXMOM, 0>(map, TP, s);
     if (per <= 2) return launch_tma_mf<MAXMOM, 2>(map, TP, s);
     if (per <= 4) return launch_tma_mf<MAXMOM, 4>(map, TP, s);
