@@ -209,6 +209,42 @@ def max_over_ranks(ms, world, dist, device="cuda"):
     return float(t.item())
 
 
+def accuracy_vs_plain(S, b, film, pb, pfilm):
+    """Error of the FP32 form against the plain FP64 form on the same samples:
+    relative error of filmD (to each pixel's largest channel) and the fraction of
+    Welch accept/reject decisions (pixel x neighbour x transform) that differ."""
+    import torch
+    w = WORKLOAD
+    R = w["radius"]
+    words = S.bits_words(R)
+    K = b.K
+    bits = []
+    for bb, ff in ((b, film), (pb, pfilm)):
+        rgb = ff.update_image()
+        if bb.precision == S.F64:
+            rgb = rgb.double()
+        t = torch.zeros(bb.H * bb.W, K, words, dtype=torch.int32, device="cuda")
+        bb.denoise_film(radius=R, filter_sd=w["filter_sd"], alpha=w["alpha"], gbuffers=_specs(S), film=rgb,
+                        accept_bits=t)
+        bits.append(t)
+    torch.cuda.synchronize()
+    v = bits[0] ^ bits[1]  # popcount of the differing decision bits, per int32 word
+    v = v - ((v >> 1) & 0x55555555)
+    v = (v & 0x33333333) + ((v >> 2) & 0x33333333)
+    v = (v + (v >> 4)) & 0x0F0F0F0F
+    v = (v & 0xFF) + ((v >> 8) & 0xFF) + ((v >> 16) & 0xFF) + ((v >> 24) & 0xFF)
+    flips = int(v.sum(dtype=torch.int64).item())
+    total = b.H * b.W * K * (2 * R + 1) ** 2
+    a = b.filmD.double()
+    r = pb.filmD.double()
+    scale = r.abs().amax(dim=0, keepdim=True).clamp_min(1e-30)
+    rel = ((a - r).abs() / scale).flatten()
+    q = float(torch.quantile(rel[torch.randperm(rel.numel(), device=rel.device)[:1 << 20]], 0.999).item())
+    del bits, v
+    return {"filmD_rel_max": float(rel.max().item()), "filmD_rel_p999": q,
+            "flipped_decisions": flips / total, "decisions": total}
+
+
 def run_gpu(args, rank, world, dist):
     import numpy as np
     import torch
@@ -341,6 +377,7 @@ def run_gpu(args, rank, world, dist):
                               "accumulate_ms": statistics.median(accs), "denoise_ms": statistics.median(dens),
                               "note": "FP64, one image per launch, sample generation excluded"}
         extra["speedup_vs_plain_f64"] = value / world / extra["plain_f64"]["value"]
+        extra["fp32_vs_fp64"] = accuracy_vs_plain(S, b, film, pb, pfilm)
         del pb, pfilm, samples_c
         torch.cuda.empty_cache()
 

@@ -1,0 +1,84 @@
+"""The benchmark's full size (1920x1080, 256 spp, K=5, G=7, 21x21 window) on the
+GPU, through properties that do not need the CPU oracle at this size:
+
+* accumulating the samples in four calls of 64 equals one call of 256, bit for
+  bit (statistics, feature means, counts and film sums persist across calls);
+* every count and film weight equals 256;
+* the FP32 form against the plain FP64 form on the same samples: denoised film
+  within 1e-4 of each pixel's largest channel at the 99.9th percentile, and at
+  most 0.1% of the Welch accept/reject decisions flipped.
+"""
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+W, H, SPP, G = 1920, 1080, 256, 7
+TR = ("identity", "log1p", "sqrt", "cbrt", "asinh")
+R = 10
+
+
+@pytest.fixture(scope="module")
+def S():
+    import stater_gb300 as S
+    S.setup()
+    return S
+
+
+@pytest.fixture(scope="module")
+def samples(S):
+    return S.generate_samples(W, H, SPP, n_features=G, seed=77)
+
+
+def _run(S, samples, precision, mode, chunks):
+    b = S.StatBuffers(W, H, TR, G, 3, precision)
+    film = S.Film(W, H, n_features=G)
+    step = SPP // chunks
+    for c in range(chunks):
+        b.accumulate(samples[c * step:(c + 1) * step], mode=mode, film=film)
+    return b, film
+
+
+def _specs(S):
+    return [S.GBufferSpec(0, 3, 0.02), S.GBufferSpec(3, 3, 0.1), S.GBufferSpec(6, 1, 0.1)]
+
+
+def test_chunked_equals_single_pass(S, samples):
+    one, f1 = _run(S, samples, S.F32, S.ACC_FAST, 1)
+    four, f4 = _run(S, samples, S.F32, S.ACC_FAST, 4)
+    torch.cuda.synchronize()
+    assert torch.equal(one.stats, four.stats) and torch.equal(one.gmean, four.gmean)
+    assert torch.equal(one.n, four.n) and bool((one.n == SPP).all())
+    assert torch.equal(f1.contrib_sum, f4.contrib_sum)
+    assert bool((f1.weight_sum + f1.spill[3] >= SPP).all()) and bool((f1.weight_sum == SPP).all())
+
+
+def _popcount_sum(v):
+    v = v - ((v >> 1) & 0x55555555)
+    v = (v & 0x33333333) + ((v >> 2) & 0x33333333)
+    v = (v + (v >> 4)) & 0x0F0F0F0F
+    v = (v & 0xFF) + ((v >> 8) & 0xFF) + ((v >> 16) & 0xFF) + ((v >> 24) & 0xFF)
+    return int(v.sum(dtype=torch.int64).item())
+
+
+def test_fp32_against_plain_fp64_full_size(S, samples):
+    words = S.bits_words(R)
+    out = []
+    for precision, mode in ((S.F32, S.ACC_FAST), (S.F64, S.ACC_EXACT)):
+        b, film = _run(S, samples, precision, mode, 4 if precision == S.F64 else 1)
+        rgb = film.update_image()
+        if precision == S.F64:
+            rgb = rgb.double()
+        b.denoise_vars(radius=R, gbuffers=_specs(S))
+        bits = torch.zeros(H * W, len(TR), words, dtype=torch.int32, device="cuda")
+        b.denoise_film(radius=R, gbuffers=_specs(S), film=rgb, accept_bits=bits)
+        torch.cuda.synchronize()
+        out.append((b.filmD.double(), bits))
+        del b, film
+    (a, ba), (r, br) = out
+    scale = r.abs().amax(dim=0, keepdim=True).clamp_min(1e-30)
+    rel = ((a - r).abs() / scale).flatten()
+    sample = rel[torch.randperm(rel.numel(), device=rel.device)[:1 << 22]]
+    assert float(torch.quantile(sample, 0.999)) <= 1e-4
+    flips = _popcount_sum(ba ^ br) / (H * W * len(TR) * (2 * R + 1) ** 2)
+    assert flips <= 1e-3
