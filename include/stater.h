@@ -244,8 +244,19 @@ typedef struct {
     void *discr[STATER_MAX_TRANSFORMS];
     void *filmD;
     uint32_t *accept_bits;
+    /* Order in which the FP32 form tests the transforms of a neighbour (it stops
+     * at the first rejection in STATER_MT_ALL mode; the result does not depend
+     * on the order). A permutation of 0..n_buffers-1, or all zero for the
+     * reverse index order. stater_test_order gives one from the transform kinds. */
+    int32_t test_order[STATER_MAX_TRANSFORMS];
 } stater_denoise_film_args;
 stater_status stater_denoise_film(const stater_denoise_film_args *a, stater_stream stream);
+
+/* A test order for stater_denoise_film_args.test_order: the most compressing
+ * transforms first (asinh, cbrt and Box-Cox with lambda < 1/2, sqrt, log1p,
+ * other Box-Cox), the untransformed set (transform 0) last; they reject most
+ * of the neighbours that any transform rejects, so the filter stops earlier. */
+stater_status stater_test_order(const stater_transform *transforms, int32_t n_transforms, int32_t *order);
 
 /* Squared two-sided Student-t critical values over u = 1/df: table[m] =
  * t_{1-alpha/2}(N/m)^2 (table[0] = z^2), m = 0..N, N = lut_intervals. The Welch

@@ -72,7 +72,8 @@ class DenoiseFilmArgs(C.Structure):
                 ("filter_radius", C.c_int32), ("ds_factor", C.c_float), ("alpha", C.c_float),
                 ("mt_mode", C.c_int32), ("use_levc", C.c_int32), ("precision", C.c_int32),
                 ("n", VP), ("film", VP), ("mean", P8), ("varD", P8), ("varCD", P8), ("jb", P8),
-                ("gbuffers", GBuffers), ("discr", P8), ("filmD", VP), ("accept_bits", VP)]
+                ("gbuffers", GBuffers), ("discr", P8), ("filmD", VP), ("accept_bits", VP),
+                ("test_order", C.c_int32 * MAX_TRANSFORMS)]
 
 
 class StaterError(RuntimeError):
@@ -122,6 +123,7 @@ def load() -> C.CDLL:
                                                 C.c_double, C.c_int32, C.c_int32, VP, VP]),
         "stater_calc_mean_var": (st, [C.c_int32, C.c_int32, VP, VP, VP, VP]),
         "stater_film_add_samples": (st, [C.POINTER(FilmArgs), VP]),
+        "stater_test_order": (st, [C.POINTER(Transform), C.c_int32, VP]),
         "stater_film_update_image": (st, [C.c_int32, C.c_int32, VP, VP, VP, C.c_float, VP, VP]),
         "stater_lev_state_size": (C.c_int32, [C.c_int32, C.c_int32]),
         "stater_lev_accumulate": (st, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, VP, VP, C.c_int32, VP, VP]),

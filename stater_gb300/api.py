@@ -183,6 +183,10 @@ class StatBuffers:
         a.filmD = _ptr(self.filmD)
         a.accept_bits = _ptr(accept_bits)
         a.gbuffers = self._gbuffers(gbuffers)
+        tr = (L.Transform * L.MAX_TRANSFORMS)()
+        for k, (kind, lam) in enumerate(self.transforms):
+            tr[k].kind, tr[k].lambda_ = kind, lam
+        L.call("stater_test_order", tr, self.K, C.cast(a.test_order, C.c_void_p))
         L.call("stater_denoise_film", C.byref(a), _stream_ptr(stream))
 
     def calc_target_spp(self, spp: int, out: torch.Tensor, relative: bool = True, eps: float = 1e-4,

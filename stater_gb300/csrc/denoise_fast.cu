@@ -89,6 +89,7 @@ struct FastFilm {
     float *discr[STATER_MAX_TRANSFORMS];
     float *filmD;
     uint32_t *bits;
+    int8_t order[STATER_MAX_TRANSFORMS];  // ring kernel: slot -> transform tested in that position
 };
 
 // ---------------------------------------------------------------------------
@@ -824,7 +825,7 @@ __device__ __forceinline__ float4 film_ring_value(const FastFilm &P, int rec, in
         if (kr == 0) {
             v = f4(__ldg(P.film + g), __ldg(P.film + HW + g), __ldg(P.film + 2 * HW + g), 0.f);
         } else {
-            const int k = (kr - 1) >> 1, sub = (kr - 1) & 1;
+            const int k = P.order[(kr - 1) >> 1], sub = (kr - 1) & 1;
             const float *mean = k == 0 ? P.film : P.mean[k];
             if (sub == 0)
                 v = f4(__ldg(mean + g), __ldg(mean + HW + g), __ldg(mean + 2 * HW + g), __ldg(P.discr[k] + g));
@@ -880,30 +881,34 @@ __global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
     int ni = in ? __ldg(P.n + gi) : 0;
     if (ni < 2) ni = 0;
     const bool act = in && ni >= 2;
+    // slots hold the transforms in test order; ksel is the slot of the JB choice
     int ksel = -1;
     if (act && P.mt_mode == STATER_MT_JB) {
-        ksel = 0;
+        int kbest = 0;
         float best = __ldg(P.jb[0] + gi);
         for (int k = 1; k < K; k++) {
             const float v = __ldg(P.jb[k] + gi);
             if (v < best) {
                 best = v;
-                ksel = k;
+                kbest = k;
             }
         }
+        for (int sl = 0; sl < K; sl++)
+            if (P.order[sl] == kbest) ksel = sl;
     }
     float fi[kRingMF];
 #pragma unroll
     for (int f = 0; f < kRingMF; f++) fi[f] = (in && f < nf) ? __ldg(P.feat.plane[f] + gi) * P.feat.mul[f] : 0.f;
     float mi[KMAX][3], di[KMAX][3];
 #pragma unroll
-    for (int k = 0; k < KMAX; k++)
+    for (int sl = 0; sl < KMAX; sl++)
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            const bool ok = in && k < K;
+            const bool ok = in && sl < K;
+            const int k = ok ? P.order[sl] : 0;
             const float *mean = k == 0 ? P.film : P.mean[k];
-            mi[k][c] = ok ? __ldg(mean + (size_t)c * HW + gi) : 0.f;
-            di[k][c] = ok ? __ldg(P.discr[k] + (size_t)c * HW + gi) : 0.f;
+            mi[sl][c] = ok ? __ldg(mean + (size_t)c * HW + gi) : 0.f;
+            di[sl][c] = ok ? __ldg(P.discr[k] + (size_t)c * HW + gi) : 0.f;
         }
     __syncthreads();
     const bool uni = s_nmin == s_nmax;
@@ -1207,6 +1212,20 @@ stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s
     }
     P.filmD = (float *)a->filmD;
     P.bits = a->accept_bits;
+    {
+        // a permutation of 0..K-1, else the reverse index order
+        bool seen[STATER_MAX_TRANSFORMS] = {false}, perm = true, zero = true;
+        for (int sl = 0; sl < P.K; sl++) {
+            const int k = a->test_order[sl];
+            if (k != 0) zero = false;
+            if (k < 0 || k >= P.K || seen[k]) perm = false;
+            else seen[k] = true;
+        }
+        if (!perm && !zero)
+            return set_error(STATER_ERR_INVALID, "stater_denoise_film: test_order is not a permutation");
+        for (int sl = 0; sl < STATER_MAX_TRANSFORMS; sl++)
+            P.order[sl] = (int8_t)(sl < P.K ? (perm && !(zero && P.K > 1) ? a->test_order[sl] : P.K - 1 - sl) : 0);
+    }
     const size_t HW = (size_t)P.W * P.H;
     if (!make_featset(P.feat, a->gbuffers, HW))
         return set_error(STATER_ERR_INVALID, "stater_denoise_film: bad gbuffers (at most 24 channels, dr_factor <= 0)");
@@ -1269,3 +1288,40 @@ stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s
 }
 
 }  // namespace stater
+
+extern "C" stater_status stater_test_order(const stater_transform *transforms, int32_t n_transforms,
+                                           int32_t *order) {
+    using namespace stater;
+    clear_error();
+    if (!transforms || !order || n_transforms < 1 || n_transforms > STATER_MAX_TRANSFORMS)
+        return set_error(STATER_ERR_INVALID, "stater_test_order: bad arguments");
+    auto rank = [&](int k) {
+        if (k == 0) return 100;  // the untransformed set last
+        // measured on the benchmark's radiance (means around 0.4): the strongly
+        // compressing transforms reject first; log1p is nearly linear there
+        const float lam = transforms[k].lambda;
+        switch (transforms[k].kind) {
+            case STATER_TK_ASINH: return 0;
+            case STATER_TK_CBRT: return 1;
+            case STATER_TK_BOXCOX: return lam < 0.5f ? 1 : (lam < 1.f ? 2 : 5);
+            case STATER_TK_SQRT: return 2;
+            case STATER_TK_LOG1P: return 3;
+            default: return 6;
+        }
+    };
+    int idx[STATER_MAX_TRANSFORMS];
+    for (int k = 0; k < n_transforms; k++) idx[k] = k;
+    // stable insertion sort by rank, then by descending index
+    for (int i = 1; i < n_transforms; i++) {
+        const int v = idx[i];
+        int j = i - 1;
+        while (j >= 0 && (rank(idx[j]) > rank(v) || (rank(idx[j]) == rank(v) && idx[j] < v))) {
+            idx[j + 1] = idx[j];
+            j--;
+        }
+        idx[j + 1] = v;
+    }
+    for (int k = 0; k < STATER_MAX_TRANSFORMS; k++) order[k] = k < n_transforms ? idx[k] : 0;
+    return STATER_OK;
+}
+

@@ -321,6 +321,7 @@ bool stater_server::enqueue_after_round(Job &j) {
         }
         f.gbuffers = gb;
         f.filmD = j.base + L.off_filmD;
+        if (stater_test_order(j.d.transforms, j.d.n_transforms, f.test_order) != STATER_OK) return false;
         if (stater_denoise_film(&f, (stater_stream)s) != STATER_OK) return false;
         if (j.d.out_host) {
             if (L.T == 4) {

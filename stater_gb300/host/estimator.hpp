@@ -335,6 +335,7 @@ class Estimator {
         }
         a.gbuffers = gbuffers(meanG);
         a.filmD = filmD_.get();
+        check(stater_test_order(cfg.transforms.data(), K, a.test_order), "Estimator::DenoiseMeans");
         check(stater_denoise_film(&a, (stater_stream)stream), "Estimator::DenoiseMeans");
     }
 
