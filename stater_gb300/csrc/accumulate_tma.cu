@@ -16,14 +16,12 @@
 #include <cuda.h>
 
 #include "acc_kernels.cuh"
+#include "tma_common.cuh"
 
 namespace stater {
-
-int *device_error_word();
-bool encode_tensor_map_2d_f32(CUtensorMap *map, const void *base, uint64_t cols, uint64_t rows, uint32_t box_cols,
-                              uint32_t box_rows);
-
 namespace {
+
+using namespace tma;
 
 #ifndef STATER_TMA_SAMPLES_PER_STAGE
 #define STATER_TMA_SAMPLES_PER_STAGE 4
@@ -34,48 +32,6 @@ namespace {
 constexpr int kPx = 32;                                // pixels per CTA (one warp-wide row of consumers per transform)
 constexpr int kSB = STATER_TMA_SAMPLES_PER_STAGE;      // samples per stage
 constexpr int kStages = STATER_TMA_STAGES;             // ring depth
-constexpr uint32_t kWaitLimit = 1u << 22;
-constexpr int kErrTimeout = 1;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-// Bounded wait for the phase with parity `parity` to complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitLimit; i++) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(smem_u32(bar)), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1, uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            smem_u32(dst)),
-        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
-        : "memory");
-}
 
 struct TmaAccParams {
     AccParams P;

@@ -96,17 +96,21 @@ __global__ void __launch_bounds__(128) lev_solve_kernel(size_t HW, const T *__re
         }
         return;
     }
-    double mean[P0], Cff[G > 0 ? G : 1][G > 0 ? G : 1], L[G > 0 ? G : 1][G > 0 ? G : 1];
+    // One reciprocal of n and of each Cholesky pivot instead of a division per
+    // term (FP64 division is a long instruction sequence on this part), and
+    // fused multiply-adds in the dot products.
+    const double inv_n = 1.0 / n;
+    double mean[P0], Cff[G > 0 ? G : 1][G > 0 ? G : 1], L[G > 0 ? G : 1][G > 0 ? G : 1], inv_d[G > 0 ? G : 1];
     double cfy[G > 0 ? G : 1][3], cyy[3];
 #pragma unroll
-    for (int a = 0; a < P0; a++) mean[a] = st[oP + a] + st[oS + a] / n;
+    for (int a = 0; a < P0; a++) mean[a] = fma(st[oS + a], inv_n, st[oP + a]);
     {
         int q = 0;
 #pragma unroll
         for (int a = 0; a < G; a++)
 #pragma unroll
             for (int b = a; b < G; b++, q++) {
-                const double v = st[oFF + q] - st[oS + a] * st[oS + b] / n;
+                const double v = fma(-st[oS + a], st[oS + b] * inv_n, st[oFF + q]);
                 Cff[a][b] = v;
                 Cff[b][a] = v;
             }
@@ -114,47 +118,49 @@ __global__ void __launch_bounds__(128) lev_solve_kernel(size_t HW, const T *__re
 #pragma unroll
     for (int a = 0; a < G; a++)
 #pragma unroll
-        for (int c = 0; c < 3; c++) cfy[a][c] = st[oFY + a * 3 + c] - st[oS + a] * st[oS + G + c] / n;
+        for (int c = 0; c < 3; c++) cfy[a][c] = fma(-st[oS + a], st[oS + G + c] * inv_n, st[oFY + a * 3 + c]);
 #pragma unroll
-    for (int c = 0; c < 3; c++) cyy[c] = st[oYY + c] - st[oS + G + c] * st[oS + G + c] / n;
+    for (int c = 0; c < 3; c++) cyy[c] = fma(-st[oS + G + c], st[oS + G + c] * inv_n, st[oYY + c]);
 #pragma unroll
     for (int a = 0; a < G; a++)
 #pragma unroll
         for (int b = 0; b <= a; b++) {
-            double sum = Cff[a][b] / n + (a == b ? lambda : 0.0);
+            double sum = fma(Cff[a][b], inv_n, a == b ? lambda : 0.0);
 #pragma unroll
-            for (int m = 0; m < b; m++) sum = sum - L[a][m] * L[b][m];
-            if (a == b)
+            for (int m = 0; m < b; m++) sum = fma(-L[a][m], L[b][m], sum);
+            if (a == b) {
                 L[a][a] = sqrt(sum > 0.0 ? sum : 1e-300);
-            else
-                L[a][b] = sum / L[b][b];
+                inv_d[a] = 1.0 / L[a][a];
+            } else {
+                L[a][b] = sum * inv_d[b];
+            }
         }
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         double tmp[G > 0 ? G : 1], bt[G > 0 ? G : 1];
 #pragma unroll
         for (int a = 0; a < G; a++) {
-            double sum = cfy[a][c] / n;
+            double sum = cfy[a][c] * inv_n;
 #pragma unroll
-            for (int m = 0; m < a; m++) sum = sum - L[a][m] * tmp[m];
-            tmp[a] = sum / L[a][a];
+            for (int m = 0; m < a; m++) sum = fma(-L[a][m], tmp[m], sum);
+            tmp[a] = sum * inv_d[a];
         }
 #pragma unroll
         for (int a = G - 1; a >= 0; a--) {
             double sum = tmp[a];
 #pragma unroll
-            for (int m = a + 1; m < G; m++) sum = sum - L[m][a] * bt[m];
-            bt[a] = sum / L[a][a];
+            for (int m = a + 1; m < G; m++) sum = fma(-L[m][a], bt[m], sum);
+            bt[a] = sum * inv_d[a];
         }
         double bc = 0.0, bab = 0.0, icpt = mean[G + c];
 #pragma unroll
         for (int a = 0; a < G; a++) {
-            bc = bc + bt[a] * cfy[a][c];
+            bc = fma(bt[a], cfy[a][c], bc);
             double row = 0.0;
 #pragma unroll
-            for (int b = 0; b < G; b++) row = row + Cff[a][b] * bt[b];
-            bab = bab + bt[a] * row;
-            icpt = icpt - bt[a] * mean[a];
+            for (int b = 0; b < G; b++) row = fma(Cff[a][b], bt[b], row);
+            bab = fma(bt[a], row, bab);
+            icpt = fma(-bt[a], mean[a], icpt);
         }
         double rss = cyy[c] - 2.0 * bc + bab;
         if (rss < 0.0) rss = 0.0;

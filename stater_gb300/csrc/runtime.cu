@@ -141,6 +141,19 @@ bool encode_tensor_map_2d_f32(CUtensorMap *map, const void *base, uint64_t cols,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+bool encode_tensor_map_3d_f32(CUtensorMap *map, const void *base, uint64_t d0, uint64_t d1, uint64_t d2, uint32_t b0,
+                              uint32_t b1, uint32_t b2) {
+    CUtensorMap probe;
+    if (!encode_tensor_map_2d_f32(&probe, base, d0, d1 * d2, b0, 1)) return false;  // resolves the entry point
+    const cuuint64_t dims[3] = {d0, d1, d2};
+    const cuuint64_t strides[2] = {d0 * 4, d0 * d1 * 4};
+    const cuuint32_t box[3] = {b0, b1, b2};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 const void *tcrit_table_device(double alpha, bool f64, cudaStream_t stream) {
     int dev = 0;
     cudaGetDevice(&dev);
