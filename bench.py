@@ -525,17 +525,25 @@ def run_config(args, rank, world, dist):
         jobs = serving_trace(args.jobs, seed=rank)
         # warm-up: one small job per slot (scratch buffers, tables)
         run_serving_trace(S, serving_trace(4, seed=99)[:4], 0, args.slots, S.F32)
+        rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
+        sweep = []
         with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
-            st = run_serving_trace(S, jobs, args.rate, args.slots, S.F32)
+            for rate in rates:
+                st = run_serving_trace(S, jobs, rate, args.slots, S.F32)
+                sweep.append({"rate_jobs_per_s": rate, "mpix_per_s": st["mpix_per_s"],
+                              "latency_p50_ms": st["latency_p50_ms"], "latency_p99_ms": st["latency_p99_ms"],
+                              "peak_footprint_gb": st["peak_footprint_bytes"] / 1e9})
+        # the headline is the highest rate of the sweep (arrivals faster than the GPU: its capacity)
         # one job at a time, plain FP64 form, on the part of the trace small enough to finish quickly
         small = [j for j in jobs if j["width"] * j["height"] * j["spp"] <= 1280 * 720 * 256][:args.f64_jobs]
         f32_small = run_serving_trace(S, small, 0, args.slots, S.F32)
         f64_small = run_serving_trace(S, small, 0, 1, S.F64, with_output=False)
-        line = {"metric": "Mpix/s served (mixed jobs, Poisson arrivals)", "value": st["mpix_per_s"], "unit": UNIT,
+        line = {"metric": "Mpix/s served (mixed jobs, Poisson arrivals)", "value": sweep[-1]["mpix_per_s"], "unit": UNIT,
                 "n_gpus": world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded on-device generation)",
                 "config": {"workload": f"{len(jobs)} jobs, resolutions {SERVE_RES}, spp {SERVE_SPP}, K {SERVE_K}",
-                           "rate_jobs_per_s": args.rate, "slots": args.slots},
+                           "rate_jobs_per_s": rates[-1], "slots": args.slots},
+                "rate_sweep": sweep,
                 "latency_ms": {"p50": st["latency_p50_ms"], "p99": st["latency_p99_ms"], "mean": st["latency_mean_ms"]},
                 "completed": st["completed"], "failed": st["failed"], "peak_footprint_gb": st["peak_footprint_bytes"] / 1e9,
                 "subset_vs_plain_f64": {"jobs": len(small), "f32_batched_mpix_s": f32_small["mpix_per_s"],
@@ -625,6 +633,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--config", default="denoise", choices=["denoise", "serving", "adaptive", "lev"])
     ap.add_argument("--rate", type=float, default=10.0, help="serving: job arrivals per second")
+    ap.add_argument("--rates", default="10,50,200,500", help="serving: comma-separated arrival rates to sweep")
     ap.add_argument("--jobs", type=int, default=40, help="serving: jobs in the trace")
     ap.add_argument("--slots", type=int, default=4, help="serving: concurrent jobs")
     ap.add_argument("--f64-jobs", type=int, default=6, help="serving: jobs timed in the plain FP64 form")

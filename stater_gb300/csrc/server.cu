@@ -65,7 +65,9 @@ int chunk_for(const stater_job_desc &d, int chunk_spp) {
     const size_t HW = (size_t)d.width * d.height;
     const size_t per = (size_t)(5 + d.n_features) * HW * 4;
     int c = std::max(1, chunk_spp > 0 ? chunk_spp : 32);
-    while (c > 1 && (size_t)c * per > ((size_t)2 << 30)) c /= 2;  // at most 2 GiB of sample planes per step
+    // at most 16 GiB of sample planes per step: a 3840x2160 job still takes 32
+    // samples per step (each step also reads and writes the whole moment state)
+    while (c > 1 && (size_t)c * per > ((size_t)16 << 30)) c /= 2;
     return c;
 }
 
