@@ -486,7 +486,7 @@ def serving_trace(njobs, seed=0):
     return jobs
 
 
-def run_serving_trace(S, jobs, rate, slots, precision, with_output=True, seed=1):
+def run_serving_trace(S, jobs, rate, slots, precision, with_output=True, seed=1, chunk=32):
     """Submits `jobs` at Poisson arrival times (rate jobs/s; rate <= 0: all at once)
     and returns the server statistics."""
     import numpy as np
@@ -495,7 +495,7 @@ def run_serving_trace(S, jobs, rate, slots, precision, with_output=True, seed=1)
     gaps = rng.exponential(1.0 / rate, len(jobs)) if rate > 0 else np.zeros(len(jobs))
     arrivals = np.cumsum(gaps)
     outs = [np.zeros((3, j["height"], j["width"]), np.float32) if with_output else None for j in jobs]
-    with serving.Server(max_slots=slots, precision=precision) as srv:
+    with serving.Server(max_slots=slots, precision=precision, chunk_spp=chunk) as srv:
         t0 = time.perf_counter()
         for j, o, at in zip(jobs, outs, arrivals):
             delay = at - (time.perf_counter() - t0)
@@ -529,7 +529,7 @@ def run_config(args, rank, world, dist):
         sweep = []
         with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
             for rate in rates:
-                st = run_serving_trace(S, jobs, rate, args.slots, S.F32)
+                st = run_serving_trace(S, jobs, rate, args.slots, S.F32, chunk=args.chunk)
                 sweep.append({"rate_jobs_per_s": rate, "mpix_per_s": st["mpix_per_s"],
                               "latency_p50_ms": st["latency_p50_ms"], "latency_p99_ms": st["latency_p99_ms"],
                               "peak_footprint_gb": st["peak_footprint_bytes"] / 1e9})
@@ -560,7 +560,7 @@ def run_config(args, rank, world, dist):
         res = {}
         for prec, name in ((S.F32, "f32"), (S.F64, "f64")):
             lat = []
-            with serving.Server(max_slots=1, precision=prec) as srv:
+            with serving.Server(max_slots=1, precision=prec, chunk_spp=args.chunk) as srv:
                 for it in range(args.warmup + args.steps if prec == S.F32 else 2):
                     out = np.zeros((3, H, W), np.float32) if prec == S.F32 else None
                     jid = srv.submit(serving.job_desc(**job, out=out), keepalive=out)
@@ -636,6 +636,7 @@ def main():
     ap.add_argument("--rates", default="10,50,200,500", help="serving: comma-separated arrival rates to sweep")
     ap.add_argument("--jobs", type=int, default=40, help="serving: jobs in the trace")
     ap.add_argument("--slots", type=int, default=4, help="serving: concurrent jobs")
+    ap.add_argument("--chunk", type=int, default=32, help="serving / adaptive: samples generated and accumulated per step")
     ap.add_argument("--f64-jobs", type=int, default=6, help="serving: jobs timed in the plain FP64 form")
     ap.add_argument("--width", type=int, default=None, help="smaller image for profiling captures")
     ap.add_argument("--height", type=int, default=None)

@@ -143,6 +143,14 @@ typedef struct {
     float *film_weight_sum;     /* [W*H] */
     float *film_spill;          /* [4][W*H] */
     float film_max_sample_luminance; /* INFINITY = off */
+    /* Optional pixel index (NULL: sample column i is pixel i): the sample planes
+     * are [S][5+G][n_active] and column i, with count[i] samples, belongs to
+     * pixel pixel_index[i]. Columns with samples must name distinct pixels;
+     * columns with count 0 (padding) and indices outside the image are skipped.
+     * Lets a caller pack only the pixels that still need samples, e.g. sorted
+     * by their adaptive target so that each launch covers a dense prefix. */
+    const int32_t *pixel_index;
+    int32_t n_active;
 } stater_accumulate_args;
 stater_status stater_accumulate(const stater_accumulate_args *a, stater_stream stream);
 
@@ -164,6 +172,11 @@ typedef struct {
     const int32_t *first_index; /* nullable */
     const int32_t *count;       /* nullable: only the first count[p] samples of pixel p are written */
     float *samples;
+    /* Optional pixel index as in stater_accumulate_args: column i of the planes
+     * [S][5+G][n_active] holds the samples of pixel pixel_index[i]; first_index
+     * and count are then per column. */
+    const int32_t *pixel_index;
+    int32_t n_active;
 } stater_generate_args;
 stater_status stater_generate_samples(const stater_generate_args *a, stater_stream stream);
 

@@ -47,7 +47,7 @@ class AccumulateArgs(C.Structure):
                 ("max_moment", C.c_int32), ("precision", C.c_int32), ("mode", C.c_int32),
                 ("n", VP), ("stats", VP), ("gmean", VP),
                 ("film_contrib_sum", VP), ("film_weight_sum", VP), ("film_spill", VP),
-                ("film_max_sample_luminance", C.c_float)]
+                ("film_max_sample_luminance", C.c_float), ("pixel_index", VP), ("n_active", C.c_int32)]
 
 
 class GenerateArgs(C.Structure):
@@ -55,7 +55,7 @@ class GenerateArgs(C.Structure):
                 ("n_features", C.c_int32), ("seed", C.c_uint64), ("region", C.c_int32),
                 ("mean_mu", C.c_float), ("mean_sigma", C.c_float), ("noise_sigma", C.c_float),
                 ("firefly_prob", C.c_float), ("firefly_scale", C.c_float), ("lev_r2", C.c_float),
-                ("first_index", VP), ("count", VP), ("samples", VP)]
+                ("first_index", VP), ("count", VP), ("samples", VP), ("pixel_index", VP), ("n_active", C.c_int32)]
 
 
 class DenoiseVarsArgs(C.Structure):

@@ -116,13 +116,19 @@ class StatBuffers:
 
     # -- stage 1 -----------------------------------------------------------------
     def accumulate(self, samples: torch.Tensor, count: Optional[torch.Tensor] = None, mode: int = L.ACC_EXACT,
-                   film: Optional["Film"] = None, stream=None) -> None:
+                   film: Optional["Film"] = None, pixel_index: Optional[torch.Tensor] = None,
+                   stream=None) -> None:
         """StatTile::AddTransformSample* over sample planes [S, 5+G, H, W] (float32);
-        with `film`, also FilmTile::AddSample of the same samples in the same pass."""
+        with `film`, also FilmTile::AddSample of the same samples in the same pass.
+        With `pixel_index` (int32 [N]), the planes are [S, 5+G, N] and column i
+        belongs to pixel pixel_index[i] (count, if given, is per column)."""
         if samples.dtype != torch.float32 or not samples.is_contiguous():
             raise ValueError("samples must be contiguous float32 [S, 5+G, H, W]")
         S = samples.shape[0]
-        if samples.shape[1:] != (5 + self.G, self.H, self.W):
+        if pixel_index is not None:
+            if samples.dim() != 3 or samples.shape[1:] != (5 + self.G, pixel_index.numel()):
+                raise ValueError("with pixel_index the samples are [S, 5+G, N]")
+        elif samples.shape[1:] != (5 + self.G, self.H, self.W):
             raise ValueError(f"samples shape {tuple(samples.shape)} does not match the buffers")
         a = L.AccumulateArgs()
         a.width, a.height, a.n_samples, a.n_features = self.W, self.H, S, self.G
@@ -133,6 +139,8 @@ class StatBuffers:
             a.transforms[k].lambda_ = lam
         a.max_moment, a.precision, a.mode = self.max_moment, self.precision, int(mode)
         a.n, a.stats, a.gmean = _ptr(self.n), _ptr(self.stats), _ptr(self.gmean)
+        if pixel_index is not None:
+            a.pixel_index, a.n_active = _ptr(pixel_index), int(pixel_index.numel())
         if film is not None:
             if (film.W, film.H, film.G) != (self.W, self.H, self.G):
                 raise ValueError("film geometry does not match the buffers")
@@ -206,16 +214,22 @@ def generate_samples(width: int, height: int, n_samples: int, n_features: int = 
                      region: int = 8, mean_mu: float = -1.0, mean_sigma: float = 1.0, noise_sigma: float = 0.5,
                      firefly_prob: float = 1e-3, firefly_scale: float = 1e3, lev_r2: float = 0.0,
                      first_index: Optional[torch.Tensor] = None, count: Optional[torch.Tensor] = None,
-                     out: Optional[torch.Tensor] = None, device="cuda", stream=None) -> torch.Tensor:
-    """Seeded synthetic sample planes [S, 5+G, H, W] generated on the device."""
+                     out: Optional[torch.Tensor] = None, pixel_index: Optional[torch.Tensor] = None,
+                     device="cuda", stream=None) -> torch.Tensor:
+    """Seeded synthetic sample planes [S, 5+G, H, W] generated on the device
+    ([S, 5+G, N] for the pixels of `pixel_index`)."""
     if out is None:
-        out = torch.empty(n_samples, 5 + n_features, height, width, dtype=torch.float32, device=device)
+        shape = (n_samples, 5 + n_features, pixel_index.numel()) if pixel_index is not None else \
+            (n_samples, 5 + n_features, height, width)
+        out = torch.empty(*shape, dtype=torch.float32, device=device)
     g = L.GenerateArgs()
     g.width, g.height, g.n_samples, g.n_features = width, height, n_samples, n_features
     g.seed, g.region = int(seed), int(region)
     g.mean_mu, g.mean_sigma, g.noise_sigma = mean_mu, mean_sigma, noise_sigma
     g.firefly_prob, g.firefly_scale, g.lev_r2 = firefly_prob, firefly_scale, lev_r2
     g.first_index, g.count, g.samples = _ptr(first_index), _ptr(count), _ptr(out)
+    if pixel_index is not None:
+        g.pixel_index, g.n_active = _ptr(pixel_index), int(pixel_index.numel())
     L.call("stater_generate_samples", C.byref(g), _stream_ptr(stream))
     return out
 

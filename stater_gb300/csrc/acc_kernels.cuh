@@ -22,7 +22,9 @@
 namespace stater {
 
 struct AccParams {
-    size_t HW;
+    size_t HW;   // sample columns (pixels, or entries of pix)
+    size_t HWs;  // pixels of the statistics planes (W*H)
+    const int32_t *pix;  // nullable: sample column i belongs to pixel pix[i]
     int S, G, K, NCH;
     const float *__restrict__ samples;
     const int32_t *__restrict__ count;
@@ -239,12 +241,12 @@ __device__ __forceinline__ void feat_update(float v, uint32_t nn, T rn, T &fm) {
 }
 
 template <typename T, bool FAST, int MAXMOM, int MAXF, int KIND>
-__device__ __forceinline__ void acc_loop(const AccParams &P, size_t p, int k, int cnt, uint32_t n0, float lam,
-                                         T (&mean)[3], T (&m2)[3], T (&m3)[3], T (&m4)[3], T (&cx)[3],
+__device__ __forceinline__ void acc_loop(const AccParams &P, size_t i, size_t p, int k, int cnt, uint32_t n0,
+                                         float lam, T (&mean)[3], T (&m2)[3], T (&m3)[3], T (&m4)[3], T (&cx)[3],
                                          T (&cy)[3], T (&m1)[3], T (&fm)[MAXF > 0 ? MAXF : 1], bool film,
                                          FilmAcc &fa) {
-    const size_t HW = P.HW;
-    const float *sp = P.samples + p;
+    const size_t HW = P.HW;  // sample column stride
+    const float *sp = P.samples + i;
     const size_t sstride = (size_t)P.NCH * HW;
     constexpr int NL = MAXMOM >= 5 ? 5 : 3;
     // The next sample's loads are issued before the current one is processed.
@@ -286,17 +288,24 @@ __device__ __forceinline__ void acc_loop(const AccParams &P, size_t p, int k, in
 
 template <typename T, bool FAST, int MAXMOM, int MAXF>
 __global__ void __launch_bounds__(256) acc_kernel(AccParams P) {
-    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // sample column i, pixel p (the same unless a pixel index is given)
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int k = threadIdx.y;
-    const bool valid = p < P.HW;
+    size_t p = i;
+    bool valid = i < P.HW;
+    if (valid && P.pix) {
+        const int32_t q = P.pix[i];
+        valid = q >= 0 && (size_t)q < P.HWs;
+        p = valid ? (size_t)q : 0;
+    }
+    // per-pixel counts beyond the S sample planes are clamped (never read past them)
+    const int cnt = valid ? (P.count ? min(max(P.count[i], 0), P.S) : P.S) : 0;
     // Every transform's thread reads n before the transform-0 thread of the same
     // pixel may write the updated count back.
-    const uint32_t n0 = valid ? (uint32_t)P.n[p] : 0u;
+    const uint32_t n0 = cnt > 0 ? (uint32_t)P.n[p] : 0u;
     __syncthreads();
-    if (!valid) return;
-    const size_t HW = P.HW;
-    // per-pixel counts beyond the S sample planes are clamped (never read past them)
-    const int cnt = P.count ? min(max(P.count[p], 0), P.S) : P.S;
+    if (cnt == 0) return;  // nothing to add: the pixel's state is neither read nor written
+    const size_t HW = P.HWs;  // statistics plane stride
     T *st = (T *)P.stats;
     T *gm = (T *)P.gmean;
 
@@ -326,15 +335,15 @@ __global__ void __launch_bounds__(256) acc_kernel(AccParams P) {
     switch (P.ts.kind[k]) {
 #define STATER_ACC_CASE(KD)                                                                                   \
     case KD:                                                                                                  \
-        acc_loop<T, FAST, MAXMOM, MAXF, KD>(P, p, k, cnt, n0, lam, mean, m2, m3, m4, cx, cy, m1, fm, film, fa); \
+        acc_loop<T, FAST, MAXMOM, MAXF, KD>(P, i, p, k, cnt, n0, lam, mean, m2, m3, m4, cx, cy, m1, fm, film, fa); \
         break;
         STATER_ACC_CASE(STATER_TK_LOG1P)
         STATER_ACC_CASE(STATER_TK_SQRT)
         STATER_ACC_CASE(STATER_TK_CBRT)
         STATER_ACC_CASE(STATER_TK_ASINH)
         STATER_ACC_CASE(STATER_TK_BOXCOX)
-        default: acc_loop<T, FAST, MAXMOM, MAXF, STATER_TK_IDENTITY>(P, p, k, cnt, n0, lam, mean, m2, m3, m4, cx,
-                                                                     cy, m1, fm, film, fa);
+        default: acc_loop<T, FAST, MAXMOM, MAXF, STATER_TK_IDENTITY>(P, i, p, k, cnt, n0, lam, mean, m2, m3, m4,
+                                                                     cx, cy, m1, fm, film, fa);
 #undef STATER_ACC_CASE
     }
     if (film) film_store(P.film, HW, p, fa);

@@ -16,6 +16,8 @@ cudaError_t launch_acc_tma_f32(const AccParams &P, int max_moment, cudaStream_t 
 // ---------------------------------------------------------------------------
 struct GenParams {
     int W, H, S, G, region;
+    const int32_t *pix;  // nullable: column i generates pixel pix[i]
+    size_t ncols;        // sample columns (W*H, or entries of pix)
     uint32_t k0, k1;
     float mean_mu, mean_sigma, noise_sigma, ff_prob, ff_scale, lev_r2, lev_b;
     const int32_t *first_index;
@@ -32,13 +34,19 @@ __device__ inline void box_muller(uint32_t a, uint32_t b, float &z0, float &z1) 
 }
 
 __global__ void generate_kernel(GenParams g) {
-    const size_t HW = (size_t)g.W * g.H;
-    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= HW) return;
+    const size_t HW = g.ncols;  // column stride of the sample planes
+    const size_t col = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= HW) return;
+    size_t p = col;
+    if (g.pix) {
+        const int32_t q = g.pix[col];
+        if (q < 0 || (size_t)q >= (size_t)g.W * g.H) return;
+        p = (size_t)q;
+    }
     const int x = (int)(p % g.W), y = (int)(p / g.W);
     const int rw = (g.W + g.region - 1) / g.region;
     const uint32_t rid = (uint32_t)((y / g.region) * rw + x / g.region);
-    const uint32_t first = g.first_index ? (uint32_t)g.first_index[p] : 0u;
+    const uint32_t first = g.first_index ? (uint32_t)g.first_index[col] : 0u;
     const int NCH = 5 + g.G;
 
     // Per-region radiance mean and feature base values.
@@ -59,10 +67,10 @@ __global__ void generate_kernel(GenParams g) {
         for (int j = 0; j < 4 && f + j < g.G; j++) base[f + j] = u01(v[j]);
     }
 
-    const int ns = g.count ? min(max(g.count[p], 0), g.S) : g.S;
+    const int ns = g.count ? min(max(g.count[col], 0), g.S) : g.S;
     for (int s = 0; s < ns; s++) {
         const uint32_t sidx = first + (uint32_t)s;
-        float *out = g.samples + (size_t)s * NCH * HW + p;
+        float *out = g.samples + (size_t)s * NCH * HW + col;
         const U4 a = philox4x32_10({(uint32_t)p, sidx, 0u, 0u}, g.k0, g.k1);
         const U4 b = philox4x32_10({(uint32_t)p, sidx, 1u, 0u}, g.k0, g.k1);
         float z[4];
@@ -224,10 +232,14 @@ stater_status stater_accumulate(const stater_accumulate_args *a, stater_stream s
             return set_error(STATER_ERR_INVALID, "stater_accumulate: unknown transform kind");
     if (a->film_contrib_sum && (!a->film_weight_sum || !a->film_spill || !(a->film_max_sample_luminance > 0.0f)))
         return set_error(STATER_ERR_INVALID, "stater_accumulate: incomplete film buffers");
+    if (a->pixel_index && a->n_active <= 0)
+        return set_error(STATER_ERR_INVALID, "stater_accumulate: pixel_index needs n_active > 0");
     if (a->n_samples == 0) return STATER_OK;
 
     AccParams P;
-    P.HW = (size_t)a->width * a->height;
+    P.HWs = (size_t)a->width * a->height;
+    P.pix = a->pixel_index;
+    P.HW = a->pixel_index ? (size_t)a->n_active : P.HWs;
     P.S = a->n_samples;
     P.G = a->n_features;
     P.K = a->n_transforms;
@@ -294,8 +306,11 @@ stater_status stater_generate_samples(const stater_generate_args *a, stater_stre
     g.first_index = a->first_index;
     g.count = a->count;
     g.samples = a->samples;
-    const size_t HW = (size_t)g.W * g.H;
-    generate_kernel<<<(unsigned)((HW + 255) / 256), 256, 0, (cudaStream_t)stream>>>(g);
+    g.pix = a->pixel_index;
+    g.ncols = a->pixel_index ? (size_t)a->n_active : (size_t)g.W * g.H;
+    if (a->pixel_index && a->n_active <= 0)
+        return set_error(STATER_ERR_INVALID, "stater_generate_samples: pixel_index needs n_active > 0");
+    generate_kernel<<<(unsigned)((g.ncols + 255) / 256), 256, 0, (cudaStream_t)stream>>>(g);
     return cuda_status(cudaGetLastError(), "stater_generate_samples launch");
 }
 

@@ -105,8 +105,8 @@ __global__ void __launch_bounds__(kPx *STATER_MAX_TRANSFORMS + 32)
     const int tid = threadIdx.x;
     const int warp = tid / 32, lane = tid % 32;
     const bool producer = warp == P.K;
-    const size_t p0 = (size_t)blockIdx.x * kPx;
-    const size_t HW = P.HW;
+    const size_t p0 = (size_t)blockIdx.x * kPx;  // first sample column of the CTA
+    const size_t HW = P.HWs;                     // statistics plane stride
 
     if (tid == 0) {
         for (int i = 0; i < kStages; i++) {
@@ -117,15 +117,24 @@ __global__ void __launch_bounds__(kPx *STATER_MAX_TRANSFORMS + 32)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    // sample column i, pixel p (the same unless a pixel index is given); a
+    // column without samples neither reads nor writes its pixel's state
+    const size_t i = p0 + lane;
+    size_t p = i;
+    bool inr = !producer && i < P.HW;
+    if (inr && P.pix) {
+        const int32_t q = P.pix[i];
+        inr = q >= 0 && (size_t)q < P.HWs;
+        p = inr ? (size_t)q : 0;
+    }
+    const int cnt = inr ? (P.count ? min(max(P.count[i], 0), P.S) : P.S) : 0;
+    const bool valid = cnt > 0;
     // Every transform's thread reads n before the transform-0 thread of the same
     // pixel may write the updated count back (the barrier below orders them).
-    const size_t p = p0 + lane;
-    const bool valid = !producer && p < HW;
     const uint32_t n0 = valid ? (uint32_t)P.n[p] : 0u;
     // Number of samples this CTA needs: the largest count among its pixels.
     if (warp == 0) {
-        int c = 0;
-        if (p < HW) c = P.count ? min(max(P.count[p], 0), P.S) : P.S;
+        int c = cnt;
         for (int o = 16; o > 0; o >>= 1) c = max(c, __shfl_xor_sync(0xffffffffu, c, o));
         if (lane == 0) s_maxcnt = c;
     }
@@ -157,7 +166,6 @@ __global__ void __launch_bounds__(kPx *STATER_MAX_TRANSFORMS + 32)
 
     // consumers: thread (pixel, transform)
     const int k = warp;
-    const int cnt = valid ? (P.count ? min(max(P.count[p], 0), P.S) : P.S) : 0;
     float *st = (float *)P.stats;
     float *gm = (float *)P.gmean;
     float mean[3], m2[3], m3[3], m4[3], cx[3], cy[3], m1[3];

@@ -34,31 +34,70 @@ using Clock = std::chrono::steady_clock;
 constexpr int kTmin = 16, kTmax = 1024;
 constexpr double kEps = 1e-4;
 
-__global__ void chunk_counts_kernel(size_t HW, const int32_t *target, int done, int chunk, int32_t *counts) {
-    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= HW) return;
-    counts[p] = max(0, min(target[p] - done, chunk));
-}
 
 __global__ void widen_kernel(size_t n, const float *in, double *out) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = (double)in[i];
 }
 
-__global__ void max_kernel(size_t HW, const int32_t *v, int32_t *out) {
-    int m = 0;
-    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < HW; p += (size_t)gridDim.x * blockDim.x)
-        m = max(m, v[p]);
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+// Adaptive rounds visit the pixels sorted by their target (descending), so
+// that the samples still due at any point belong to a prefix of the order and
+// each step covers only that prefix (a 32-pixel group no longer runs to the
+// largest target among its neighbours). Counting sort over targets 0..kTmax.
+constexpr int kBins = 1025;  // targets 0..kTmax
+
+__global__ void target_hist_kernel(size_t HW, const int32_t *target, int32_t *hist) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= HW) return;
+    atomicAdd(&hist[min(max(target[p], 0), kBins - 1)], 1);
 }
+
+// One thread: cursor[t] = number of pixels with a target above t (the first
+// position of bin t in the descending order); act[c] = pixels whose target
+// exceeds c * chunk (the active prefix of step c), c = 0..nsteps; *tmax.
+__global__ void target_scan_kernel(const int32_t *hist, int chunk, int32_t *cursor, int32_t *act, int32_t *tmax) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    int32_t above = 0, mx = 0;
+    for (int t = kBins - 1; t >= 0; t--) {
+        cursor[t] = above;
+        if (hist[t] > 0 && mx == 0) mx = t;
+        above += hist[t];
+    }
+    *tmax = mx;
+    const int nsteps = (kBins - 1 + chunk - 1) / chunk;
+    for (int c = 0; c <= nsteps; c++) {
+        const int d = c * chunk;
+        act[c] = d < kBins ? cursor[d] : 0;
+    }
+}
+
+__global__ void target_scatter_kernel(size_t HW, const int32_t *target, int32_t *cursor, int32_t *order,
+                                      int32_t *tsorted) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= HW) return;
+    const int t = min(max(target[p], 0), kBins - 1);
+    const int i = atomicAdd(&cursor[t], 1);
+    order[i] = (int32_t)p;
+    tsorted[i] = t;
+}
+
+// Per column of step `done`: samples due (0 for padding beyond the active
+// prefix) and the pixel's next sample index.
+__global__ void sorted_step_kernel(int ncols, const int32_t *order, const int32_t *tsorted, const int32_t *n,
+                                   int done, int chunk, int32_t *counts, int32_t *first) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ncols) return;
+    counts[i] = max(0, min(tsorted[i] - done, chunk));
+    first[i] = n[order[i]];
+}
+
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct Layout {
     size_t HW, T, K, G, chunk;
-    size_t off_n, off_counts, off_target, off_max, off_stats, off_gmean, off_film, off_rgb, off_rgb64, off_jb, off_out6,
-        off_filmD, off_samples, total;
+    size_t off_n, off_counts, off_target, off_max, off_order, off_tsorted, off_first, off_hist, off_cursor, off_act,
+        off_stats, off_gmean, off_film, off_rgb, off_rgb64, off_jb, off_out6, off_filmD, off_samples, total;
 };
 
 int chunk_for(const stater_job_desc &d, int chunk_spp) {
@@ -85,9 +124,15 @@ Layout layout(const stater_job_desc &d, int precision, int chunk_spp) {
         return r;
     };
     L.off_n = take(4 * L.HW);
-    L.off_counts = take(4 * L.HW);
+    L.off_counts = take(4 * (L.HW + 4));
     L.off_target = take(4 * L.HW);
     L.off_max = take(4);
+    L.off_order = take(4 * (L.HW + 4));
+    L.off_tsorted = take(4 * (L.HW + 4));
+    L.off_first = take(4 * (L.HW + 4));
+    L.off_hist = take(4 * kBins);
+    L.off_cursor = take(4 * kBins);
+    L.off_act = take(4 * (kBins + 2));
     L.off_stats = take(L.K * STATER_NQ * 3 * L.HW * L.T);
     L.off_gmean = take(std::max<size_t>(L.G, 1) * L.HW * L.T);
     L.off_film = take(8 * L.HW * 4);  // film sums: contrib[3], weight, spill[4]
@@ -96,7 +141,7 @@ Layout layout(const stater_job_desc &d, int precision, int chunk_spp) {
     L.off_jb = take(L.K * L.HW * L.T);
     L.off_out6 = take(6 * L.K * 3 * L.HW * L.T);
     L.off_filmD = take(3 * L.HW * L.T);
-    L.off_samples = take(L.chunk * (5 + L.G) * L.HW * 4);
+    L.off_samples = take(L.chunk * (5 + L.G) * (L.HW + 4) * 4);  // + 4 columns: a padded active prefix
     L.total = o;
     return L;
 }
@@ -127,6 +172,7 @@ struct Job {
 struct Slot {
     cudaStream_t stream = nullptr;
     int32_t *hmax = nullptr;  // pinned: largest target of the last round
+    int32_t *hact = nullptr;  // pinned: active prefix length of each step of the next round
     bool busy = false;
 };
 
@@ -189,12 +235,19 @@ bool stater_server::enqueue_round(Job &j, int samples, bool uniform) {
     const Layout &L = j.L;
     int32_t *n = (int32_t *)(j.base + L.off_n);
     int32_t *counts = (int32_t *)(j.base + L.off_counts);
-    int32_t *target = (int32_t *)(j.base + L.off_target);
     float *smp = (float *)(j.base + L.off_samples);
-    for (int done = 0; done < samples; done += (int)L.chunk) {
+    const int32_t *order = (const int32_t *)(j.base + L.off_order);
+    int32_t *first = (int32_t *)(j.base + L.off_first);
+    for (int done = 0, step = 0; done < samples; done += (int)L.chunk, step++) {
         const int S = std::min((int)L.chunk, samples - done);
+        // adaptive round: the active prefix of the sorted order, padded to 4 columns
+        int ncols = 0;
         if (!uniform) {
-            chunk_counts_kernel<<<(unsigned)((L.HW + 255) / 256), 256, 0, s>>>(L.HW, target, done, S, counts);
+            const int active = sl.hact[step];
+            if (active <= 0) break;
+            ncols = std::min((int)L.HW + 4, (active + 3) / 4 * 4);
+            sorted_step_kernel<<<(unsigned)((ncols + 255) / 256), 256, 0, s>>>(ncols, order, (const int32_t *)(j.base + L.off_tsorted),
+                                                                              n, done, S, counts, first);
             if (cudaGetLastError() != cudaSuccess) return false;
         }
         stater_generate_args g{};
@@ -209,9 +262,13 @@ bool stater_server::enqueue_round(Job &j, int samples, bool uniform) {
         g.noise_sigma = 0.5f;
         g.firefly_prob = 1e-3f;
         g.firefly_scale = 1e3f;
-        g.first_index = n;  // every pixel continues its own sample sequence
+        g.first_index = uniform ? n : first;  // every pixel continues its own sample sequence
         g.count = uniform ? nullptr : counts;  // only the samples the accumulation will read
         g.samples = smp;
+        if (!uniform) {
+            g.pixel_index = order;
+            g.n_active = ncols;
+        }
         if (stater_generate_samples(&g, (stater_stream)s) != STATER_OK) return false;
         stater_accumulate_args a{};
         a.width = j.d.width;
@@ -233,6 +290,10 @@ bool stater_server::enqueue_round(Job &j, int samples, bool uniform) {
         a.film_weight_sum = fs + 3 * L.HW;
         a.film_spill = fs + 4 * L.HW;
         a.film_max_sample_luminance = INFINITY;
+        if (!uniform) {
+            a.pixel_index = order;
+            a.n_active = ncols;
+        }
         if (stater_accumulate(&a, (stater_stream)s) != STATER_OK) return false;
     }
     return true;
@@ -283,11 +344,20 @@ bool stater_server::enqueue_after_round(Job &j) {
         if (stater_calc_target_spp(j.d.width, j.d.height, budget, prec_of(this), v.n, v.varD[0], moment(0, STATER_Q_MEAN),
                                    kEps, kTmin, kTmax, target, (stater_stream)s) != STATER_OK)
             return false;
+        // pixels sorted by target; the largest target and each step's active prefix to the host
         int32_t *dmax = (int32_t *)(j.base + L.off_max);
-        if (cudaMemsetAsync(dmax, 0, 4, s) != cudaSuccess) return false;
-        max_kernel<<<std::max(1, std::min(1024, (int)((L.HW + 255) / 256))), 256, 0, s>>>(L.HW, target, dmax);
+        int32_t *hist = (int32_t *)(j.base + L.off_hist);
+        int32_t *cursor = (int32_t *)(j.base + L.off_cursor);
+        int32_t *act = (int32_t *)(j.base + L.off_act);
+        const unsigned blocks = (unsigned)((L.HW + 255) / 256);
+        if (cudaMemsetAsync(hist, 0, 4 * kBins, s) != cudaSuccess) return false;
+        target_hist_kernel<<<blocks, 256, 0, s>>>(L.HW, target, hist);
+        target_scan_kernel<<<1, 1, 0, s>>>(hist, (int)L.chunk, cursor, act, dmax);
+        target_scatter_kernel<<<blocks, 256, 0, s>>>(L.HW, target, cursor, (int32_t *)(j.base + L.off_order),
+                                                     (int32_t *)(j.base + L.off_tsorted));
         if (cudaGetLastError() != cudaSuccess) return false;
         if (cudaMemcpyAsync(sl.hmax, dmax, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return false;
+        if (cudaMemcpyAsync(sl.hact, act, 4 * (kBins + 2), cudaMemcpyDeviceToHost, s) != cudaSuccess) return false;
     } else {
         // Film::UpdateImage: the film image is the untransformed mean that denoiseFilm filters
         const float *fs = (const float *)(j.base + L.off_film);
@@ -473,7 +543,8 @@ stater_status stater_server_create(const stater_server_config *cfg, stater_serve
     s->slots.resize(cfg->max_slots);
     for (auto &sl : s->slots) {
         if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaMallocHost(&sl.hmax, sizeof(int32_t)) != cudaSuccess) {
+            cudaMallocHost(&sl.hmax, sizeof(int32_t)) != cudaSuccess ||
+            cudaMallocHost(&sl.hact, sizeof(int32_t) * (kBins + 2)) != cudaSuccess) {
             cudaGetLastError();
             delete s;
             return set_error(STATER_ERR_CUDA, "stater_server_create: stream or pinned allocation failed");
@@ -599,6 +670,7 @@ stater_status stater_server_destroy(stater_server *srv) {
             cudaStreamDestroy(sl.stream);
         }
         if (sl.hmax) cudaFreeHost(sl.hmax);
+        if (sl.hact) cudaFreeHost(sl.hact);
     }
     delete srv;
     return STATER_OK;

@@ -1,0 +1,71 @@
+"""Accumulation over a pixel index (sample column i belongs to pixel
+pixel_index[i]), as the serving engine uses it for adaptive rounds: the same
+pixels, samples and counts give the same bits as the dense layout, in any
+column order, with padding columns (count 0) skipped; the generator in index
+mode writes the same samples as the dense one."""
+import numpy as np
+import pytest
+
+from helpers import synth_samples
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TR = ("identity", "log1p", "sqrt", "cbrt", "asinh")
+
+
+@pytest.fixture(scope="module")
+def S():
+    import stater_gb300 as S
+    S.setup()
+    return S
+
+
+@pytest.mark.parametrize("W,H,precision,mode,pad", [
+    (64, 40, "F32", "ACC_FAST", 0),    # 2560 columns: TMA-fed path
+    (64, 40, "F32", "ACC_FAST", 3),    # 2563 columns: plain path
+    (50, 30, "F64", "ACC_EXACT", 2),
+])
+def test_index_mode_equals_dense(S, W, H, precision, mode, pad):
+    G, N = 7, 24
+    rng = np.random.default_rng(91)
+    s1 = synth_samples(W, H, N, G=G, seed=92)
+    cnt = rng.integers(0, N + 1, size=(H, W)).astype(np.int32)
+    prec, md = getattr(S, precision), getattr(S, mode)
+    # dense reference: one uniform round, then a round with uneven counts
+    dense = S.StatBuffers(W, H, TR, G, 5, prec)
+    fd = S.Film(W, H, G)
+    dense.accumulate(torch.from_numpy(s1).cuda(), mode=md, film=fd)
+    s2 = synth_samples(W, H, N, G=G, seed=93)
+    dense.accumulate(torch.from_numpy(s2).cuda(), count=torch.from_numpy(cnt).cuda(), mode=md, film=fd)
+    # index mode: the same first round dense, the second over a shuffled index with padding
+    idx = S.StatBuffers(W, H, TR, G, 5, prec)
+    fi = S.Film(W, H, G)
+    idx.accumulate(torch.from_numpy(s1).cuda(), mode=md, film=fi)
+    perm = rng.permutation(W * H).astype(np.int32)
+    order = np.concatenate([perm, np.zeros(pad, np.int32)])
+    ccol = np.concatenate([cnt.reshape(-1)[perm], np.zeros(pad, np.int32)])
+    planes = s2.reshape(N, 5 + G, W * H)[:, :, order].copy()
+    idx.accumulate(torch.from_numpy(planes).cuda(), count=torch.from_numpy(ccol).cuda(), mode=md, film=fi,
+                   pixel_index=torch.from_numpy(order).cuda())
+    torch.cuda.synchronize()
+    assert torch.equal(dense.n, idx.n)
+    assert torch.equal(dense.stats, idx.stats)
+    assert torch.equal(dense.gmean, idx.gmean)
+    assert torch.equal(fd.contrib_sum, fi.contrib_sum) and torch.equal(fd.weight_sum, fi.weight_sum)
+
+
+def test_generator_index_mode(S):
+    W, H, N, G = 48, 20, 12, 7
+    first = torch.arange(W * H, dtype=torch.int32, device="cuda").remainder(5).reshape(H, W).contiguous()
+    dense = S.generate_samples(W, H, N, G, seed=4, first_index=first)
+    perm = torch.from_numpy(np.random.default_rng(95).permutation(W * H).astype(np.int32)).cuda()
+    firstc = first.reshape(-1)[perm.long()].contiguous()
+    cnt = torch.full((W * H,), N, dtype=torch.int32, device="cuda")
+    cnt[::3] = 4
+    packed = S.generate_samples(W, H, N, G, seed=4, first_index=firstc, count=cnt, pixel_index=perm)
+    torch.cuda.synchronize()
+    d = dense.reshape(N, 5 + G, W * H)[:, :, perm.long()]
+    for i in (0, 1, 2, 3, 100, W * H - 1):
+        c = int(cnt[i])
+        assert torch.equal(packed[:c, :, i], d[:c, :, i])
