@@ -24,10 +24,10 @@ namespace {
 using namespace tma;
 
 #ifndef STATER_TMA_SAMPLES_PER_STAGE
-#define STATER_TMA_SAMPLES_PER_STAGE 4
+#define STATER_TMA_SAMPLES_PER_STAGE 12
 #endif
 #ifndef STATER_TMA_STAGES
-#define STATER_TMA_STAGES 4
+#define STATER_TMA_STAGES 2
 #endif
 constexpr int kPx = 32;                                // pixels per CTA (one warp-wide row of consumers per transform)
 constexpr int kSB = STATER_TMA_SAMPLES_PER_STAGE;      // samples per stage
