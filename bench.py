@@ -199,6 +199,15 @@ def _reset(b, film):
     film.clear()
 
 
+def hbm_peak_gbs():
+    """The measured STREAM-style copy bandwidth of this GPU model, else the fallback figure."""
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        return float(peaks["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured)"
+    except Exception:
+        return 6800.0, "fallback"
+
+
 def max_over_ranks(ms, world, dist, device="cuda"):
     """The largest of the ranks' timings: the job is as slow as its slowest replica."""
     import torch
@@ -317,21 +326,20 @@ def run_gpu(args, rank, world, dist):
     # roofline of the accumulation kernel (HBM-bound): algorithmic bytes per launch
     acc_bytes = HW * (SPP * (5 + G) * 4 + 2 * (K * 3 * w["max_moment"] * 4 + G * 4 + 4 + 4 * 4))
     acc_ms = statistics.median(stage_ms["accumulate"])
-    peaks = {}
-    try:
-        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
-    except Exception:
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    # DRAM bytes per launch from one ncu capture of acc_tma_kernel at 480x272, 64 spp
-    # (431.5 MB read + 27.0 MB written, film sums included), scaled by the
-    # pixel-samples of this launch.
-    traffic = (431.457536e6 + 26.955776e6) * (HW * SPP) / (480 * 272 * 64) / 1e9
+    hbm_peak, peak_source = hbm_peak_gbs()
+    # DRAM bytes per launch from one ncu capture of acc_tma_kernel at 480x272, 64 spp,
+    # K=5, G=7, M1-M3: 431.0 MB read + 23.3 MB written, film sums included. The
+    # per-pixel state (228 B each way) is scaled by pixels, the rest of the reads
+    # (the sample planes) by pixel-samples.
+    cap_px = 480 * 272
+    state_rd = cap_px * (K * 3 * w["max_moment"] * 4 + G * 4 + 4 + 4 * 4)
+    samp_rd = 430.975744e6 - state_rd
+    traffic = (samp_rd * (HW * SPP) / (cap_px * 64) + (state_rd + 23.305984e6) * HW / cap_px) / 1e9
     roofline = {"kernel": "acc_tma_kernel (stage-1 accumulation)", "bound": "hbm",
                 "achieved": acc_bytes / (acc_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                 "frac": acc_bytes / (acc_ms / 1e3) / 1e9 / hbm_peak, "traffic": traffic,
                 "algorithmic_gb": acc_bytes / 1e9,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback"}
+                "peak_source": peak_source}
 
     del samples
     torch.cuda.empty_cache()
@@ -578,8 +586,8 @@ def run_config(args, rank, world, dist):
                 "plain_f64": {"ms_per_job": res["f64"][0], "value": W * H / res["f64"][0] / 1e3},
                 "speedup_vs_plain_f64": res["f64"][0] / ms}
     elif args.config == "lev":
-        W, H, SPP, G = 1920, 1080, 512, 7
-        # all 512 samples resident (51 GB of planes) and accumulated in one call
+        W, H, SPP, G = args.width or 1920, args.height or 1080, args.spp or 512, 7
+        # all 512 samples resident (51 GB of planes at 1080p) and accumulated in one call
         chunks = [S.generate_samples(W, H, SPP, n_features=G, seed=9, lev_r2=0.6)]
         res = {}
         stream = torch.cuda.current_stream()
@@ -603,16 +611,24 @@ def run_config(args, rank, world, dist):
             res[name + "_acc"] = statistics.median(acc_times[-args.steps:]) if prec == S.F32 else acc_times[-1]
             res[name + "_r2"] = float(lev.r2.double().median().item())
         acc_bytes = W * H * SPP * (G + 3) * 4
+        acc_gbs = acc_bytes / (res["f32_acc"] / 1e3) / 1e9
+        hbm_peak, peak_source = hbm_peak_gbs()
+        # DRAM bytes per launch from one ncu capture of lev_tma_f32 at 480x272, 64 spp:
+        # 406.1 MB read + 58.7 MB written, of which the per-pixel state is 58.7 MB each
+        # way (scaled by pixels) and the rest sample planes (scaled by pixel-samples).
+        state_b, samp_b = 58.726656e6, 406.123520e6 - 58.726656e6
+        traffic = (2 * state_b * (W * H) / (480 * 272) + samp_b * (W * H * SPP) / (480 * 272 * 64)) / 1e9
         line = {"metric": "Mpix/s LEV regression (1080p, 512 spp, 7 features)", "value": W * H / res["f32"] / 1e3,
                 "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["f32"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (compensated) + f64 solve",
                 "data": "synthetic (seeded, radiance linear in the features, target R^2 0.6)",
-                "config": {"workload": "1920x1080, 512 spp, ridge lambda 1e-6, samples resident in HBM (51 GB of "
-                                       "planes, 42 GB read by the regression)"},
+                "config": {"workload": f"{W}x{H}, {SPP} spp, ridge lambda 1e-6, samples resident in HBM "
+                                       f"({W * H * SPP * (5 + G) * 4 / 1e9:.1f} GB of planes, "
+                                       f"{acc_bytes / 1e9:.1f} GB read by the regression)"},
                 "stage_ms": {"accumulate": res["f32_acc"], "solve": res["f32"] - res["f32_acc"]},
-                "roofline": {"kernel": "lev_tma_f32", "bound": "hbm",
-                             "achieved": acc_bytes / (res["f32_acc"] / 1e3) / 1e9, "unit": "GB/s",
-                             "algorithmic_gb": acc_bytes / 1e9},
+                "roofline": {"kernel": "lev_tma_f32", "bound": "hbm", "achieved": acc_gbs, "peak": hbm_peak,
+                             "unit": "GB/s", "frac": acc_gbs / hbm_peak, "traffic": traffic,
+                             "algorithmic_gb": acc_bytes / 1e9, "peak_source": peak_source},
                 "median_r2": res["f32_r2"], "plain_f64": {"ms_per_step": res["f64"], "median_r2": res["f64_r2"]},
                 "speedup_vs_plain_f64": res["f64"] / res["f32"]}
     if rank == 0 and line is not None:

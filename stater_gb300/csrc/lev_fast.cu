@@ -131,8 +131,14 @@ __global__ void __launch_bounds__(kPx *kParts) lev_acc_f32(size_t HW, int S, con
 // stage instead of global memory. Same arithmetic and the same 8-sample
 // compensation blocks as lev_acc_f32, so the state is bit-identical.
 // ---------------------------------------------------------------------------
-constexpr int kLSB = 4;     // samples per stage
-constexpr int kLStages = 4;
+#ifndef STATER_LEV_SAMPLES_PER_STAGE
+#define STATER_LEV_SAMPLES_PER_STAGE 2
+#endif
+#ifndef STATER_LEV_STAGES
+#define STATER_LEV_STAGES 4
+#endif
+constexpr int kLSB = STATER_LEV_SAMPLES_PER_STAGE;  // samples per stage (divides the 8-sample blocks)
+constexpr int kLStages = STATER_LEV_STAGES;
 
 template <int G, int QLO, int QHI>
 __device__ __forceinline__ bool lev_tma_consume(const float *stages, int stage_floats, uint64_t *full, uint64_t *empty,
