@@ -18,6 +18,7 @@
 
 #include "common.cuh"
 #include "film_common.cuh"
+#include "packed_f32x2.cuh"
 
 namespace stater {
 
@@ -56,8 +57,8 @@ inline float acc_kind_cost(int kind) {
 }
 
 // Assigns the G feature channels to transforms (greedily to the cheapest
-// current load; transform 0 also carries the film). Returns the largest
-// number of channels one transform keeps.
+// current load, at most ceil(G/K) each; transform 0 also carries the film).
+// Returns the largest number of channels one transform keeps.
 inline int acc_assign_features(AccParams &P) {
     float load[STATER_MAX_TRANSFORMS];
     int cnt[STATER_MAX_TRANSFORMS];
@@ -67,10 +68,11 @@ inline int acc_assign_features(AccParams &P) {
         for (int j = 0; j < STATER_MAX_FEATURES; j++) P.featmap[k][j] = -1;
     }
     int maxc = 0;
+    const int cap = (P.G + P.K - 1) / P.K;  // no transform keeps more than its share
     for (int g = 0; g < P.G; g++) {
-        int best = 0;
-        for (int k = 1; k < P.K; k++)
-            if (load[k] < load[best]) best = k;
+        int best = -1;
+        for (int k = 0; k < P.K; k++)
+            if (cnt[k] < cap && (best < 0 || load[k] < load[best])) best = k;
         P.featmap[best][cnt[best]++] = (int8_t)g;
         load[best] += 0.15f;
         if (cnt[best] > maxc) maxc = cnt[best];
@@ -78,8 +80,14 @@ inline int acc_assign_features(AccParams &P) {
     return maxc;
 }
 
-// Compact FP32 forms used by the FAST mode (few instructions, no slow paths;
-// accurate to a few 1e-7 relative, checked against the FP64 oracle):
+// Compact FP32 forms used by the FAST mode, written once over the value type V
+// (float, or F2 = two pixels in one register with packed arithmetic) from
+// explicitly rounded operations and the hardware approximations, so the
+// scalar and packed kernels give the same bits. No addition or subtraction
+// takes a product as an operand (such pairs are written as FMAs): the code
+// generator may fuse a packed multiply into a following packed add, never a
+// scalar one with explicit rounding, so the sequence leaves it nothing to
+// fuse. Accurate to a few 1e-7 relative, checked against the FP64 oracle:
 //   log1p: 2 atanh(t), t = x/(2+x), by its Taylor series t + t^3/3 + t^5/5
 //          for x < 1/4 (t < 1/9; truncation below 4e-7 relative), else
 //          log2(1+x) ln 2 with the hardware log2;
@@ -88,6 +96,7 @@ inline int acc_assign_features(AccParams &P) {
 //          (2|x| above 1e18, where x^2 would overflow), odd;
 //   cbrt:  2^(log2|x| / 3) refined by one Newton step, odd;
 //   sqrt:  x * rsqrt(x).
+// Divisions are a multiplication by the hardware reciprocal.
 __device__ __forceinline__ float fast_log2(float x) {
     float y;
     asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -98,73 +107,130 @@ __device__ __forceinline__ float fast_exp2(float x) {
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
-__device__ __forceinline__ float log1p_compact(float x) {
-    const float t = __fdividef(x, 2.f + x);
-    const float t2 = t * t;
-    float p = fmaf(t2, 1.f / 5.f, 1.f / 3.f);
-    p = fmaf(t2, p, 1.f);
-    const float small = 2.f * t * p;
-    const float large = fast_log2(1.f + x) * 0.69314718055994531f;
-    return x < 0.25f ? small : large;
+__device__ __forceinline__ float fast_rcp(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
-__device__ __forceinline__ float asinh_compact(float x) {
-    const float a = fabsf(x);
-    const float a2 = a * a;
-    float p = fmaf(a2, -5.f / 112.f, 3.f / 40.f);
-    p = fmaf(a2, p, -1.f / 6.f);
-    p = fmaf(a2, p, 1.f);
-    const float small = a * p;
-    const float v = fmaf(a, a, 1.f);
-    const float t = a > 1e18f ? 2.f * a : a + v * rsqrtf(v);
-    const float large = fast_log2(t) * 0.69314718055994531f;
-    return copysignf(a < 0.25f ? small : large, x);
+__device__ __forceinline__ float fast_rsqrt(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
-__device__ __forceinline__ float cbrt_compact(float x) {
-    const float a = fabsf(x);
-    if (!(a > 0.f)) return x;
-    float y = fast_exp2(fast_log2(a) * (1.f / 3.f));
-    y = y - __fdividef(y * y * y - a, 3.f * y * y);
-    return copysignf(y, x);
+
+constexpr float kLn2f = 0.69314718055994531f;
+
+template <typename V>
+__device__ __forceinline__ V log1p_compact(V x) {
+    const V t = vmul(x, vmap(vadd(vconst<V>(2.f), x), fast_rcp));
+    const V t2 = vmul(t, t);
+    V q = vfma(t2, vconst<V>(1.f / 5.f), vconst<V>(1.f / 3.f));
+    q = vfma(t2, q, vconst<V>(1.f));
+    const V small = vmul(vmul(vconst<V>(2.f), t), q);
+    const V large = vmul(vmap(vadd(vconst<V>(1.f), x), fast_log2), vconst<V>(kLn2f));
+    return vmap(x, small, large, [](float a, float s, float l) { return a < 0.25f ? s : l; });
+}
+template <typename V>
+__device__ __forceinline__ V asinh_compact(V x) {
+    const V a = vmap(x, [](float v) { return fabsf(v); });
+    const V a2 = vmul(a, a);
+    V q = vfma(a2, vconst<V>(-5.f / 112.f), vconst<V>(3.f / 40.f));
+    q = vfma(a2, q, vconst<V>(-1.f / 6.f));
+    q = vfma(a2, q, vconst<V>(1.f));
+    const V small = vmul(a, q);
+    const V w = vfma(a, a, vconst<V>(1.f));
+    const V arg = vmap(a, vfma(w, vmap(w, fast_rsqrt), a),
+                       [](float m, float t) { return m > 1e18f ? __fmul_rn(2.f, m) : t; });
+    const V large = vmul(vmap(arg, fast_log2), vconst<V>(kLn2f));
+    const V mag = vmap(a, small, large, [](float m, float s, float l) { return m < 0.25f ? s : l; });
+    return vmap(mag, x, [](float m, float v) { return copysignf(m, v); });
+}
+template <typename V>
+__device__ __forceinline__ V cbrt_compact(V x) {
+    const V a = vmap(x, [](float v) { return fabsf(v); });
+    const V na = vmap(x, [](float v) { return -fabsf(v); });
+    V y = vmap(vmul(vmap(a, fast_log2), vconst<V>(1.f / 3.f)), fast_exp2);
+    const V y2 = vmul(y, y);
+    // Newton step y - (y^3 - a) / (3 y^2)
+    y = vfma(vfma(y2, y, na), vmap(vmul(vconst<V>(-3.f), y2), fast_rcp), y);
+    return vmap(x, a, y, [](float v, float m, float r) { return m > 0.f ? copysignf(r, v) : v; });
+}
+template <typename V>
+__device__ __forceinline__ V sqrt_compact(V x) {
+    const V r = vmul(x, vmap(x, fast_rsqrt));
+    return vmap(x, r, [](float v, float s) { return v > 0.f ? s : (v == 0.f ? 0.f : __int_as_float(0x7fffffff)); });
+}
+
+// FAST transform of one radiance value (V = float or F2).
+template <typename V, int KIND>
+__device__ __forceinline__ V fast_transform(float lambda, V x) {
+    switch (KIND) {
+        case STATER_TK_LOG1P: return log1p_compact(x);
+        case STATER_TK_SQRT: return sqrt_compact(x);
+        case STATER_TK_CBRT: return cbrt_compact(x);
+        case STATER_TK_ASINH: return asinh_compact(x);
+        case STATER_TK_BOXCOX:
+            // expm1(l ln x)/l: no cancellation for small l
+            return vmap(x, [lambda](float v) { return lambda == 1.f ? v : expm1f(lambda * logf(v)) / lambda; });
+        default: return x;
+    }
 }
 
 // Transform of one radiance value. EXACT: the libm-accurate functions (and the
-// reference's (x^l - 1)/l for Box-Cox). FAST (FP32 only): the compact forms
-// above, and Box-Cox as expm1(l ln x)/l (no cancellation for small l).
+// reference's (x^l - 1)/l for Box-Cox). FAST (FP32 only): the compact forms.
 template <typename T, bool FAST, int KIND>
 __device__ __forceinline__ T acc_transform(float lambda, T x) {
     if (!FAST || sizeof(T) == 8) {
         return transform_exact<T>(KIND, lambda, x);
     } else {
-        const float xf = (float)x;
-        switch (KIND) {
-            case STATER_TK_LOG1P: return (T)log1p_compact(xf);
-            case STATER_TK_SQRT: return (T)(xf > 0.f ? xf * rsqrtf(xf) : (xf == 0.f ? 0.f : sqrtf(xf)));
-            case STATER_TK_CBRT: return (T)cbrt_compact(xf);
-            case STATER_TK_ASINH: return (T)asinh_compact(xf);
-            case STATER_TK_BOXCOX:
-                if (lambda == 1.f) return x;
-                return (T)(expm1f(lambda * logf(xf)) / lambda);
-            default: return x;
+        return (T)fast_transform<float, KIND>(lambda, (float)x);
+    }
+}
+
+// FAST update of one channel's moments by one sample. rn = 1/n, dN = d/n.
+// For a pixel's first sample (n = 1, rn = 1, moments 0) the sequence gives
+// mean = x and leaves every moment exactly 0 for finite x: every increment
+// carries the factor e = d - dN, the single rounding of d - d = 0. The reference's order: m2 updated first, m3 with the new
+// m2 (d (d^2 - dN^2) = d (d - dN)(d + dN)), m4 with the new m3 and m2,
+// c2X/c2Y with the new mean, m1 += sqrt(d (d - dN)). The transforms end in a
+// select or a sign operation, so x itself is never a product.
+template <typename V, int MAXMOM>
+__device__ __forceinline__ void meng_fast(V x, V rn, V xD, V yD, V &mean, V &m2, V &m3, V &m4, V &cx, V &cy,
+                                          V &m1) {
+    const V d = vsub(x, mean);
+    const V dN = vmul(d, rn);
+    mean = vfma(d, rn, mean);
+    if (MAXMOM >= 2) {
+        const V e = vfma(d, vmul(rn, vconst<V>(-1.f)), d);  // d - dN
+        m2 = vfma(d, e, m2);
+        if (MAXMOM >= 3) {
+            const V u = vmul(d, vmul(e, vfma(d, rn, d)));
+            const V m3n = vadd(m3, vfma(vmul(vconst<V>(-3.f), dN), m2, u));
+            if (MAXMOM >= 4) {
+                const V dN2 = vmul(dN, dN);
+                // d^3 - dN^3 = (d - dN)(d^2 + d dN + dN^2): exactly 0 with e at n = 1
+                const V c3 = vmul(e, vfma(d, d, vfma(d, dN, dN2)));
+                m4 = vadd(m4, vfma(d, c3, vfma(vmul(vconst<V>(-4.f), dN), m3n, vmul(vmul(vconst<V>(-6.f), dN2), m2))));
+            }
+            m3 = m3n;
+        }
+        if (MAXMOM >= 5) {
+            const V xm = vsub(x, mean);
+            cx = vfma(xm, xD, cx);
+            cy = vfma(xm, yD, cy);
+            m1 = vadd(m1, vmap(vmul(d, e), [](float q) { return __fsqrt_rn(q); }));
         }
     }
 }
 
-// One sample's update of one transform's moments for one channel. PEELED: the
-// caller handles a pixel's first sample separately (acc_first), so nn >= 2.
-template <typename T, bool FAST, int MAXMOM, bool PEELED = false>
-__device__ __forceinline__ void acc_update1(T x, uint32_t nn, T rn, float xD, float yD, T &mean, T &m2, T &m3, T &m4,
+// EXACT update of one transform's moments for one channel: the reference's
+// arithmetic (division by n; compiled with -fmad=false).
+template <typename T, int MAXMOM>
+__device__ __forceinline__ void acc_update1(T x, uint32_t nn, float xD, float yD, T &mean, T &m2, T &m3, T &m4,
                                             T &cx, T &cy, T &m1) {
     const T nT = (T)nn;
-    if (FAST && !PEELED && nn == 1u) {
-        // First sample: the update reduces to mean = x with every central
-        // moment exactly 0. Taking that directly keeps FMA contraction from
-        // leaving rounding residue of the size of x^3 in m3 (the EXACT form
-        // computes the reference's update, which gives 0 here as well).
-        mean = x;
-        return;
-    }
     const T d = x - mean;
-    const T dN = FAST ? d * rn : d / nT;
+    const T dN = d / nT;
     if (MAXMOM <= 1) {
         mean = mean + dN;
     } else if (MAXMOM == 2) {
@@ -186,58 +252,49 @@ __device__ __forceinline__ void acc_update1(T x, uint32_t nn, T rn, float xD, fl
 }
 
 // One sample's update of one transform's moments (3 channels). `cur` holds
-// R, G, B and, with MAXMOM >= 5, the in-pixel offsets u, v.
-template <typename T, bool FAST, int MAXMOM, int KIND, bool PEELED = false>
+// R, G, B and, with MAXMOM >= 5, the in-pixel offsets u, v. FAST: rn_out
+// receives 1/nn for the feature means.
+template <typename T, bool FAST, int MAXMOM, int KIND>
 __device__ __forceinline__ void acc_update(const float *cur, uint32_t nn, float lam, T (&mean)[3], T (&m2)[3],
                                            T (&m3)[3], T (&m4)[3], T (&cx)[3], T (&cy)[3], T (&m1)[3], T &rn_out) {
-    T rn = T(0);
-    if (FAST) {
-        // hardware reciprocal (within 1 ulp): one instruction instead of the
-        // correctly rounded sequence; the first sample never uses it
-        float r;
-        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float)nn));
-        rn = sizeof(T) == 4 ? (T)r : T(1) / (T)nn;
-    }
-    rn_out = rn;
-    float xD = 0.f, yD = 0.f;
-    if (MAXMOM >= 5) {
-        xD = cur[3] - 0.5f;
-        yD = cur[4] - 0.5f;
-    }
+    if constexpr (FAST && sizeof(T) == 4) {
+        const float rn = fast_rcp((float)nn);
+        rn_out = rn;
+        float xD = 0.f, yD = 0.f;
+        if (MAXMOM >= 5) {
+            xD = __fsub_rn(cur[3], 0.5f);
+            yD = __fsub_rn(cur[4], 0.5f);
+        }
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-        const T x = acc_transform<T, FAST, KIND>(lam, (T)cur[c]);
-        acc_update1<T, FAST, MAXMOM, PEELED>(x, nn, rn, xD, yD, mean[c], m2[c], m3[c], m4[c], cx[c], cy[c], m1[c]);
-    }
-}
-
-// FAST form, a pixel's first sample (n becomes 1): the update reduces to
-// mean = x with every central moment 0 (they are 0 already), so the sample
-// loop that follows needs no first-sample test.
-template <int KIND, typename T>
-__device__ __forceinline__ void acc_first(const float *cur, float lam, T (&mean)[3]) {
+        for (int c = 0; c < 3; c++)
+            meng_fast<float, MAXMOM>(fast_transform<float, KIND>(lam, cur[c]), rn, xD, yD, mean[c], m2[c], m3[c],
+                                     m4[c], cx[c], cy[c], m1[c]);
+    } else {
+        rn_out = T(0);
+        float xD = 0.f, yD = 0.f;
+        if (MAXMOM >= 5) {
+            xD = cur[3] - 0.5f;
+            yD = cur[4] - 0.5f;
+        }
 #pragma unroll
-    for (int c = 0; c < 3; c++) mean[c] = (T)acc_transform<float, true, KIND>(lam, cur[c]);
-}
-
-// FAST transform chosen at run time (the kind is uniform across a warp).
-__device__ __forceinline__ float fast_transform_rt(int kind, float lam, float x) {
-    switch (kind) {
-        case STATER_TK_LOG1P: return acc_transform<float, true, STATER_TK_LOG1P>(lam, x);
-        case STATER_TK_SQRT: return acc_transform<float, true, STATER_TK_SQRT>(lam, x);
-        case STATER_TK_CBRT: return acc_transform<float, true, STATER_TK_CBRT>(lam, x);
-        case STATER_TK_ASINH: return acc_transform<float, true, STATER_TK_ASINH>(lam, x);
-        case STATER_TK_BOXCOX: return acc_transform<float, true, STATER_TK_BOXCOX>(lam, x);
-        default: return x;
+        for (int c = 0; c < 3; c++) {
+            const T x = acc_transform<T, false, KIND>(lam, (T)cur[c]);
+            acc_update1<T, MAXMOM>(x, nn, xD, yD, mean[c], m2[c], m3[c], m4[c], cx[c], cy[c], m1[c]);
+        }
     }
 }
 
-// Running mean of a feature channel (AddSampleM1 of a G-buffer tile).
+// Running mean of a feature channel (AddSampleM1 of a G-buffer tile). FAST:
+// fm + (v - fm) / n with the reciprocal, fused; EXACT: the division.
 template <typename T, bool FAST>
 __device__ __forceinline__ void feat_update(float v, uint32_t nn, T rn, T &fm) {
-    const T d = (T)v - fm;
-    const T dN = FAST ? d * rn : d / (T)nn;
-    fm = fm + dN;
+    if constexpr (FAST && sizeof(T) == 4) {
+        fm = vfma(vsub(v, fm), rn, fm);
+    } else {
+        const T d = (T)v - fm;
+        const T dN = d / (T)nn;
+        fm = fm + dN;
+    }
 }
 
 template <typename T, bool FAST, int MAXMOM, int MAXF, int KIND>
@@ -271,13 +328,7 @@ __device__ __forceinline__ void acc_loop(const AccParams &P, size_t i, size_t p,
             film_add(P.film, p, cur[0], cur[1], cur[2], u, v, fa);
         }
         T rn;
-        if (FAST && nn == 1u) {
-            // first sample: mean = x; the feature means take the sample (rn = 1)
-            acc_first<KIND>(cur, lam, mean);
-            rn = T(1);
-        } else {
-            acc_update<T, FAST, MAXMOM, KIND, FAST>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
-        }
+        acc_update<T, FAST, MAXMOM, KIND>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
 #pragma unroll
         for (int jf = 0; jf < MAXF; jf++) {
             const int g = P.featmap[k][jf];

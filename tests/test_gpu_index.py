@@ -21,27 +21,43 @@ def S():
     return S
 
 
-@pytest.mark.parametrize("W,H,precision,mode,pad", [
-    (64, 40, "F32", "ACC_FAST", 0),    # 2560 columns: TMA-fed path
-    (64, 40, "F32", "ACC_FAST", 3),    # 2563 columns: plain path
-    (50, 30, "F64", "ACC_EXACT", 2),
+TR_BC = ("identity", ("boxcox", 0.3), "asinh")
+
+
+@pytest.mark.parametrize("W,H,precision,mode,pad,mm,G,tr", [
+    (64, 40, "F32", "ACC_FAST", 0, 5, 7, TR),     # 2560 columns: TMA-fed path (dense and index)
+    (64, 40, "F32", "ACC_FAST", 3, 5, 7, TR),     # 2563 columns: plain path against the TMA-fed dense call
+    (64, 40, "F32", "ACC_FAST", 3, 1, 7, TR),
+    (64, 40, "F32", "ACC_FAST", 3, 2, 7, TR),
+    (64, 40, "F32", "ACC_FAST", 3, 3, 7, TR),
+    (64, 40, "F32", "ACC_FAST", 3, 4, 7, TR),
+    (64, 40, "F32", "ACC_FAST", 3, 3, 16, TR_BC),  # more feature channels per warp, Box-Cox
+    (50, 30, "F64", "ACC_EXACT", 2, 5, 7, TR),
 ])
-def test_index_mode_equals_dense(S, W, H, precision, mode, pad):
-    G, N = 7, 24
+def test_index_mode_equals_dense(S, W, H, precision, mode, pad, mm, G, tr):
+    """The TMA-fed FP32 kernel (two columns per lane, packed arithmetic) and the
+    plain FP32 kernel give the same bits: the dense call takes the TMA-fed path
+    when W*H is a multiple of 4, the index call with padding the plain one."""
+    N = 24
     rng = np.random.default_rng(91)
     s1 = synth_samples(W, H, N, G=G, seed=92)
     cnt = rng.integers(0, N + 1, size=(H, W)).astype(np.int32)
+    # first round: uneven counts with some pixels left empty, so that the second
+    # round mixes first samples and continuing pixels within a column pair
+    cnt1 = rng.integers(0, N + 1, size=(H, W)).astype(np.int32)
+    cnt1[:, ::5] = 0
+    c1 = torch.from_numpy(cnt1).cuda()
     prec, md = getattr(S, precision), getattr(S, mode)
-    # dense reference: one uniform round, then a round with uneven counts
-    dense = S.StatBuffers(W, H, TR, G, 5, prec)
+    # dense reference: a round with uneven counts, then a second one
+    dense = S.StatBuffers(W, H, tr, G, mm, prec)
     fd = S.Film(W, H, G)
-    dense.accumulate(torch.from_numpy(s1).cuda(), mode=md, film=fd)
+    dense.accumulate(torch.from_numpy(s1).cuda(), count=c1, mode=md, film=fd)
     s2 = synth_samples(W, H, N, G=G, seed=93)
     dense.accumulate(torch.from_numpy(s2).cuda(), count=torch.from_numpy(cnt).cuda(), mode=md, film=fd)
     # index mode: the same first round dense, the second over a shuffled index with padding
-    idx = S.StatBuffers(W, H, TR, G, 5, prec)
+    idx = S.StatBuffers(W, H, tr, G, mm, prec)
     fi = S.Film(W, H, G)
-    idx.accumulate(torch.from_numpy(s1).cuda(), mode=md, film=fi)
+    idx.accumulate(torch.from_numpy(s1).cuda(), count=c1, mode=md, film=fi)
     perm = rng.permutation(W * H).astype(np.int32)
     order = np.concatenate([perm, np.zeros(pad, np.int32)])
     ccol = np.concatenate([cnt.reshape(-1)[perm], np.zeros(pad, np.int32)])
