@@ -328,13 +328,13 @@ def run_gpu(args, rank, world, dist):
     acc_ms = statistics.median(stage_ms["accumulate"])
     hbm_peak, peak_source = hbm_peak_gbs()
     # DRAM bytes per launch from one ncu capture of acc_tma_kernel at 480x272, 64 spp,
-    # K=5, G=7, M1-M3: 431.0 MB read + 23.3 MB written, film sums included. The
+    # K=5, G=7, M1-M3: 433.1 MB read + 30.7 MB written, film sums included. The
     # per-pixel state (228 B each way) is scaled by pixels, the rest of the reads
     # (the sample planes) by pixel-samples.
     cap_px = 480 * 272
     state_rd = cap_px * (K * 3 * w["max_moment"] * 4 + G * 4 + 4 + 4 * 4)
-    samp_rd = 430.975744e6 - state_rd
-    traffic = (samp_rd * (HW * SPP) / (cap_px * 64) + (state_rd + 23.305984e6) * HW / cap_px) / 1e9
+    samp_rd = 433.055488e6 - state_rd
+    traffic = (samp_rd * (HW * SPP) / (cap_px * 64) + (state_rd + 30.747136e6) * HW / cap_px) / 1e9
     roofline = {"kernel": "acc_tma_kernel (stage-1 accumulation)", "bound": "hbm",
                 "achieved": acc_bytes / (acc_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                 "frac": acc_bytes / (acc_ms / 1e3) / 1e9 / hbm_peak, "traffic": traffic,

@@ -32,10 +32,10 @@ namespace {
 using namespace tma;
 
 #ifndef STATER_TMA_SAMPLES_PER_STAGE
-#define STATER_TMA_SAMPLES_PER_STAGE 8
+#define STATER_TMA_SAMPLES_PER_STAGE 12
 #endif
 #ifndef STATER_TMA_STAGES
-#define STATER_TMA_STAGES 3
+#define STATER_TMA_STAGES 2
 #endif
 #ifndef STATER_TMA_MIN_BLOCKS
 #define STATER_TMA_MIN_BLOCKS 2
