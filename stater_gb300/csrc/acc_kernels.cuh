@@ -188,9 +188,11 @@ __device__ __forceinline__ T acc_transform(float lambda, T x) {
 }
 
 // FAST update of one channel's moments by one sample. rn = 1/n, dN = d/n.
-// For a pixel's first sample (n = 1, rn = 1, moments 0) the sequence gives
-// mean = x and leaves every moment exactly 0 for finite x: every increment
-// carries the factor e = d - dN, the single rounding of d - d = 0. The reference's order: m2 updated first, m3 with the new
+// For a pixel's first sample (n = 1, moments 0) the sequence gives mean = x
+// and leaves every moment exactly 0 for finite x: every increment carries the
+// factor e = d - dN, the single rounding of d - d = 0. This takes the hardware
+// reciprocal of 1 to be exactly 1 (checked on the GPU by the first-sample test
+// of the edge-case suite). The reference's order: m2 updated first, m3 with the new
 // m2 (d (d^2 - dN^2) = d (d - dN)(d + dN)), m4 with the new m3 and m2,
 // c2X/c2Y with the new mean, m1 += sqrt(d (d - dN)). The transforms end in a
 // select or a sign operation, so x itself is never a product.

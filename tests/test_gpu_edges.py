@@ -116,3 +116,17 @@ def test_sixteen_feature_channels(st):
         b.accumulate(dev(s), mode=mode)
         gm = host(b.gmean).astype(np.float64)
         assert np.max(_rel(gm, go, 1e-6)) <= tol
+
+
+@pytest.mark.parametrize("W,H", [(64, 32), (37, 23)])  # TMA-fed and plain FP32 kernels
+def test_fast_first_sample_is_exact(st, W, H):
+    """FAST form, a pixel's first sample: the update runs with n = 1 and the
+    hardware reciprocal of 1, and must leave every central moment exactly 0
+    and the identity mean equal to the sample (no special case in the code)."""
+    s = synth_samples(W, H, 1, G=7, seed=86, region=2)
+    b = st.StatBuffers(W, H, TR5, 7, 5, st.F32)
+    b.accumulate(dev(s), mode=st.ACC_FAST)
+    stats = host(b.stats)  # [K][7][3][H][W]
+    assert np.array_equal(stats[0, 0], s[0, 0:3])
+    assert not np.any(stats[:, 1:])
+    assert np.array_equal(host(b.n), np.ones((H, W), np.int32))
