@@ -2,8 +2,10 @@
 // pivot-shifted cross-products in plain FP32 registers, then folds the block
 // into a compensated (hi, lo) pair per sum kept in shared memory
 // (hi + lo is the running total; lo carries what the FP32 addition of hi lost).
-// Four threads share a pixel, each keeping a quarter of the sums, so the
-// per-thread state is small enough for many resident warps.
+// kParts threads (two) share a pixel, each keeping its share of the sums: the
+// per-thread state stays small enough for many resident warps, while each
+// thread's loads and pivot shifts serve half the sums (four parts: 11.3 ms,
+// two: 9.2 ms, one: 12.3 ms at 1080p / 512 spp; the sums are the same bits).
 // State planes: hi [NS][HW] followed by lo [NS][HW]; n and the pivot live in
 // the hi planes. The FP64 solve (lev.cu) reads hi + lo.
 #include "common.cuh"
@@ -16,7 +18,10 @@ __host__ __device__ constexpr int lev_nstate_f(int G) { return 1 + 2 * (G + 3) +
 
 constexpr int kBlockSamples = 8;
 constexpr int kPx = 32;    // pixels per CTA (one warp row per part of the sums)
-constexpr int kParts = 4;  // threads per pixel, each keeping a quarter of the sums
+#ifndef STATER_LEV_PARTS
+#define STATER_LEV_PARTS 2
+#endif
+constexpr int kParts = STATER_LEV_PARTS;  // threads per pixel (1 to 4), each keeping a share of the sums
 
 __host__ __device__ constexpr int lev_nsum(int G) { return lev_nstate_f(G) - (1 + (G + 3)); }
 __host__ __device__ constexpr int lev_part(int G) { return (lev_nsum(G) + kParts - 1) / kParts; }
