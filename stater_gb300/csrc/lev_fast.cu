@@ -137,10 +137,10 @@ __global__ void __launch_bounds__(kPx *kParts) lev_acc_f32(size_t HW, int S, con
 // compensation blocks as lev_acc_f32, so the state is bit-identical.
 // ---------------------------------------------------------------------------
 #ifndef STATER_LEV_SAMPLES_PER_STAGE
-#define STATER_LEV_SAMPLES_PER_STAGE 2
+#define STATER_LEV_SAMPLES_PER_STAGE 4
 #endif
 #ifndef STATER_LEV_STAGES
-#define STATER_LEV_STAGES 4
+#define STATER_LEV_STAGES 3
 #endif
 constexpr int kLSB = STATER_LEV_SAMPLES_PER_STAGE;  // samples per stage (divides the 8-sample blocks)
 constexpr int kLStages = STATER_LEV_STAGES;
