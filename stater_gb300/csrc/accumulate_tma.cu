@@ -4,9 +4,9 @@
 // HW columns. A CTA owns kPx = 64 consecutive sample columns; one producer
 // thread streams stages of kSB samples x (5+G) channels x kPx columns (one or
 // a few boxes of whole samples) into a kStages-deep ring in shared memory
-// with cp.async.bulk.tensor,
-// completing on per-stage mbarriers. One consumer warp per transform reads the
-// stages; each lane owns two neighbouring columns and keeps both pixels'
+// with cp.async.bulk.tensor, completing on per-stage mbarriers. One consumer
+// warp per transform reads the stages (the transform-0 warp also adds the film
+// sums); each lane owns two neighbouring columns and keeps both pixels'
 // moments in the halves of 64-bit registers, updated by the packed FP32
 // instructions (one issue per pair) with 8-byte shared-memory loads. The
 // update is the same operation sequence as the plain FAST kernel's (the
