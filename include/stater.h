@@ -122,7 +122,11 @@ stater_status stater_release_cache(void);
  *   stats: precision-typed [K][7][3][W*H] (transform, moment, channel, pixel)
  *   gmean: precision-typed [G][W*H] running mean of every feature channel
  *          (AddSampleM1 of the G-buffer tiles, statpath.cpp:366-379); may be NULL if G == 0
- * max_moment: 1..5 as the reference's "maxmoment" (statpath.cpp:36-60; 5 = M4 + c2X, c2Y, m1). */
+ * max_moment: 1..5 as the reference's "maxmoment" (statpath.cpp:36-60; 5 = M4 + c2X, c2Y, m1).
+ * FP32 with STATER_ACC_FAST reads the planes through the Tensor Memory
+ * Accelerator when the column count is a multiple of 4 and `samples` is
+ * 16-byte aligned, and through plain loads otherwise; both forms give the same
+ * bits. */
 typedef struct {
     int32_t width, height;
     int32_t n_samples;          /* S */
