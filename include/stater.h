@@ -99,7 +99,10 @@ typedef struct {
 /* stat_denoiser::setup(): selects the current device, checks that it is an
  * sm_103 part and prepares per-device state. Idempotent. */
 stater_status stater_setup(void);
-/* stat_denoiser::synchronize(stream). */
+/* stat_denoiser::synchronize(stream). Also reports, once, STATER_ERR_TIMEOUT
+ * when a bounded wait of a TMA-fed kernel gave up since the last call (the
+ * affected call's results are incomplete; the message says whether the final
+ * wait for copies in flight gave up too), and clears that state. */
 stater_status stater_synchronize(stater_stream stream);
 /* stat_denoiser::printMacroConfiguration(): prints the runtime configuration
  * that replaces the reference's compile-time macros. */
@@ -107,7 +110,20 @@ void stater_print_macro_configuration(void);
 /* Message of the last failing call on this thread ("" if none). */
 const char *stater_last_error(void);
 int32_t stater_abi_version(void);
-/* Releases cached device scratch and tables of the current device. */
+/* Test hook for the bounded waits of the TMA-fed pipelines (the FP32
+ * stater_accumulate and stater_lev_accumulate kernels); no counterpart in the
+ * reference, which has no such pipelines. wait_polls limits every pipeline wait
+ * (0 = the default, 4,194,304 polls of mbarrier.try_wait); stall_producers = 1
+ * makes their producers issue no copies, so that the consumers' waits run out
+ * and the kernels end early, leaving STATER_ERR_TIMEOUT for stater_synchronize
+ * (stalling requires wait_polls <= 65536). The producer's final wait for copies
+ * it has issued always keeps the default limit. Settings are process-wide and
+ * apply to launches made after the call. */
+stater_status stater_debug_set_pipeline_waits(uint32_t wait_polls, int32_t stall_producers);
+/* Releases cached device scratch and tables of the current device and forgets
+ * the cached device addresses of the library's fixed arrays. Call it before a
+ * device reset (cudaDeviceReset) that is followed by further calls into the
+ * library: the cached buffers and addresses do not survive the reset. */
 stater_status stater_release_cache(void);
 
 /* ---- stage 1: moment accumulation ------------------------------------- */

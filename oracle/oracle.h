@@ -9,8 +9,11 @@
  * own code and is pinned bit-for-bit against that code compiled in place
  * (oracle/build_ref.sh -> tests/golden/). Stages 2-3 (variance denoise, Welch
  * mean filter, LEV, target-SPP) have no source in the reference tree (the CUDA
- * denoiser lives in an absent submodule); they restate the formulas documented
- * in DESIGN.md and are "parity unpinned" against the reference.
+ * denoiser lives in an absent submodule); they restate formulas written from the
+ * reference's buffer semantics (README.md:290-346) and standard statistics
+ * (Bonett's ln s^2 interval, Welch's t with Welch-Satterthwaite df, Jarque-Bera,
+ * ridge least squares), each stated beside its function in oracle.c, and are
+ * "parity unpinned" against the reference.
  *
  * Every function exists in an f64 form (the FP64 restatement, equivalent to a
  * PBRT_FLOAT_AS_DOUBLE build of the reference) and, where the reference computes
@@ -89,7 +92,10 @@ void orc_denoise_film_f64(int W, int H, int K, const int32_t *n, const double *s
 /* calcTargetSPP: next-round extra samples per pixel. */
 void orc_calc_target_spp(int W, int H, int spp, const int32_t *n, const double *varD,
                          const double *mean, double eps, int tmin, int tmax, int32_t *target);
-/* Deterministic reduction used by calcTargetSPP (block tree). */
+/* Deterministic reduction used by calcTargetSPP: the values are summed in
+ * blocks of 1024 (each block: 256 partial sums of 4 strided values, then a
+ * pairwise halving tree), and the block sums again the same way until one value
+ * is left; the GPU's reduction uses the same tree. */
 double orc_tree_sum(const double *v, int64_t len);
 
 /* Estimator::calcMatMeanVar (estimator.cpp:462-474), float arithmetic. */

@@ -108,6 +108,7 @@ def load() -> C.CDLL:
         "stater_last_error": (C.c_char_p, []),
         "stater_abi_version": (C.c_int32, []),
         "stater_release_cache": (st, []),
+        "stater_debug_set_pipeline_waits": (st, [C.c_uint32, C.c_int32]),
         "stater_accumulate": (st, [C.POINTER(AccumulateArgs), VP]),
         "stater_generate_samples": (st, [C.POINTER(GenerateArgs), VP]),
         "stater_merge_tiles": (st, [C.c_int32, C.c_int32, C.c_int32, VP, VP, C.c_int32, VP, VP, VP]),

@@ -20,7 +20,7 @@ TRANSFORM_NAMES = {"identity": L.TK_IDENTITY, "log1p": L.TK_LOG1P, "sqrt": L.TK_
                    "cbrt": L.TK_CBRT, "asinh": L.TK_ASINH, "boxcox": L.TK_BOXCOX}
 
 # The five monotone transforms of the multi-transform configuration.
-BASELINE_TRANSFORMS = (("identity", 1.0), ("log1p", 1.0), ("sqrt", 1.0), ("cbrt", 1.0), ("asinh", 1.0))
+MULTI_TRANSFORMS = (("identity", 1.0), ("log1p", 1.0), ("sqrt", 1.0), ("cbrt", 1.0), ("asinh", 1.0))
 # The reference's default single Box-Cox build: t0 raw + t1 Box-Cox(0.25) (estimator.h:48-56).
 REFERENCE_TRANSFORMS = (("identity", 1.0), ("boxcox", 0.25))
 
@@ -70,7 +70,7 @@ GBUFFERS_ALL7 = (GBufferSpec(0, 3, 0.02), GBufferSpec(3, 3, 0.1), GBufferSpec(6,
 class StatBuffers:
     """Device buffers of one image: moments, feature means and denoiser outputs."""
 
-    def __init__(self, width: int, height: int, transforms=BASELINE_TRANSFORMS, n_features: int = 7,
+    def __init__(self, width: int, height: int, transforms=MULTI_TRANSFORMS, n_features: int = 7,
                  max_moment: int = 3, precision: int = L.F32, device="cuda"):
         self.W, self.H = int(width), int(height)
         self.HW = self.W * self.H

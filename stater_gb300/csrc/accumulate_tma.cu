@@ -17,10 +17,12 @@
 // Every sample byte crosses HBM once, and kStages boxes per CTA are always in
 // flight, independent of the consumers' register use.
 //
-// Every wait is bounded. A wait that gives up records kErrTimeout in the
-// library's device error word (reported by stater_synchronize), releases what
-// it holds and lets the CTA finish; the producer first waits, again bounded,
-// for the boxes it has issued.
+// Every wait is bounded. A pipeline wait that gives up records kErrTimeout in
+// the library's device error word (reported by stater_synchronize), releases
+// what it holds and lets the CTA finish. Before it exits, the producer always
+// waits for the last boxes it issued to land (on success as well: consumers
+// that gave up may already have left), by the full kWaitLimit; if that wait
+// gives up too it records kErrDrain.
 #include <cuda.h>
 
 #include "acc_kernels.cuh"
@@ -51,7 +53,9 @@ constexpr int kUnroll = STATER_TMA_UNROLL;         // unroll of the packed loop 
 struct TmaAccParams {
     AccParams P;
     int *err;
-    int spb;  // samples per TMA box (a divisor of kSB; a box has at most 256 rows)
+    int spb;              // samples per TMA box (a divisor of kSB; a box has at most 256 rows)
+    uint32_t wait_limit;  // polls of a pipeline wait
+    int stall;            // 1: the producer issues nothing (test hook: the consumers' waits run out)
 };
 
 // Film sums of a column pair (low half: the lane's first column).
@@ -192,8 +196,9 @@ __device__ __forceinline__ void sample_one(const AccParams &P, const float *row,
 // sample loop: one specialised loop per kind, chosen once per warp; FILM: the
 // warp also adds the film sums). Returns false when a wait gave up.
 template <int MAXMOM, int MAXF, int KIND, bool FILM>
-__device__ __forceinline__ bool tma_consume(const AccParams &P, const float *stages, int stage_floats, uint64_t *full,
-                                            uint64_t *empty, int nchunks, const int (&cnt)[2],
+__device__ __forceinline__ bool tma_consume(const AccParams &P, uint32_t wait_limit, const float *stages,
+                                            int stage_floats, uint64_t *full, uint64_t *empty, int nchunks,
+                                            const int (&cnt)[2],
                                             const uint32_t (&n0)[2], const size_t (&p)[2],
                                             const int (&foff)[MAXF > 0 ? MAXF : 1], int lane, float lam,
                                             PairState<MAXF> &S) {
@@ -201,7 +206,7 @@ __device__ __forceinline__ bool tma_consume(const AccParams &P, const float *sta
     constexpr int NL = MAXMOM >= 5 ? 5 : 3;
     for (int c = 0; c < nchunks; c++) {
         const int sidx = c % kStages;
-        if (!mbar_wait(&full[sidx], (c / kStages) & 1)) return false;
+        if (!mbar_wait(&full[sidx], (c / kStages) & 1, wait_limit)) return false;
         const float *stage = stages + (size_t)sidx * stage_floats + 2 * lane;
         const int ja = min(kSB, max(0, cnt[0] - c * kSB));
         const int jb = min(kSB, max(0, cnt[1] - c * kSB));
@@ -320,9 +325,9 @@ __global__ void __launch_bounds__(32 * STATER_MAX_TRANSFORMS + 32, acc_tma_min_b
             const uint32_t bytes = (uint32_t)stage_floats * 4u;
             int issued = 0;
             bool ok = true;
-            for (int c = 0; c < nchunks && ok; c++) {
+            for (int c = 0; c < nchunks && ok && !TP.stall; c++) {
                 const int st = c % kStages;
-                if (c >= kStages) ok = mbar_wait(&empty[st], ((c / kStages) - 1) & 1);
+                if (c >= kStages) ok = mbar_wait(&empty[st], ((c / kStages) - 1) & 1, TP.wait_limit);
                 if (!ok) break;
                 mbar_arrive_expect_tx(&full[st], bytes);
                 for (int b = 0; b < kSB; b += TP.spb)
@@ -330,11 +335,13 @@ __global__ void __launch_bounds__(32 * STATER_MAX_TRANSFORMS + 32, acc_tma_min_b
                                 (c * kSB + b) * NCH, &full[st]);
                 issued = c + 1;
             }
-            if (!ok) {
-                atomicExch(TP.err, kErrTimeout);
-                // wait (bounded) for the boxes still in flight before leaving
-                for (int c = max(0, issued - kStages); c < issued; c++) mbar_wait(&full[c % kStages], (c / kStages) & 1);
-            }
+            if (!ok) atomicOr(TP.err, kErrTimeout);
+            // the last kStages boxes issued (each on its own stage, at its final
+            // phase) must have landed before the CTA may end
+            bool drained = true;
+            for (int c = max(0, issued - kStages); c < issued; c++)
+                drained = mbar_wait(&full[c % kStages], (c / kStages) & 1) && drained;
+            if (!drained) atomicOr(TP.err, kErrDrain);
         }
         return;
     }
@@ -381,8 +388,8 @@ __global__ void __launch_bounds__(32 * STATER_MAX_TRANSFORMS + 32, acc_tma_min_b
     switch (kind) {
 #define STATER_TMA_CASE(KD)                                                                                           \
     case KD:                                                                                                          \
-        ok = tma_consume<MAXMOM, MAXF, KD, false>(P, stages, stage_floats, full, empty, nchunks, cnt, n0, p, foff, lane, \
-                                                  lam, S);                                                             \
+        ok = tma_consume<MAXMOM, MAXF, KD, false>(P, TP.wait_limit, stages, stage_floats, full, empty, nchunks, cnt, n0, \
+                                                  p, foff, lane, lam, S);                                              \
         break;
         STATER_TMA_CASE(STATER_TK_LOG1P)
         STATER_TMA_CASE(STATER_TK_SQRT)
@@ -391,13 +398,15 @@ __global__ void __launch_bounds__(32 * STATER_MAX_TRANSFORMS + 32, acc_tma_min_b
         STATER_TMA_CASE(STATER_TK_BOXCOX)
 #undef STATER_TMA_CASE
         default:
-            ok = film ? tma_consume<MAXMOM, MAXF, STATER_TK_IDENTITY, true>(P, stages, stage_floats, full, empty, nchunks,
-                                                                            cnt, n0, p, foff, lane, lam, S)
-                      : tma_consume<MAXMOM, MAXF, STATER_TK_IDENTITY, false>(P, stages, stage_floats, full, empty,
-                                                                             nchunks, cnt, n0, p, foff, lane, lam, S);
+            ok = film ? tma_consume<MAXMOM, MAXF, STATER_TK_IDENTITY, true>(P, TP.wait_limit, stages, stage_floats, full,
+                                                                            empty, nchunks, cnt, n0, p, foff, lane,
+                                                                            lam, S)
+                      : tma_consume<MAXMOM, MAXF, STATER_TK_IDENTITY, false>(P, TP.wait_limit, stages, stage_floats,
+                                                                             full, empty, nchunks, cnt, n0, p, foff,
+                                                                             lane, lam, S);
     }
     if (!ok) {
-        if (lane == 0) atomicExch(TP.err, kErrTimeout);
+        if (lane == 0) atomicOr(TP.err, kErrTimeout);
         return;
     }
     auto st2 = [&](float *base, F2 v) {
@@ -479,6 +488,8 @@ cudaError_t launch_acc_tma_f32(const AccParams &P, int max_moment, cudaStream_t 
     TP.spb = spb;
     TP.err = device_error_word();
     if (!TP.err) return cudaErrorMemoryAllocation;
+    TP.wait_limit = pipeline_wait_limit();
+    TP.stall = pipeline_stall();
     switch (max_moment) {
         case 1: return launch_tma_m<1>(map, TP, s);
         case 2: return launch_tma_m<2>(map, TP, s);

@@ -1094,6 +1094,20 @@ cudaError_t set_smem(KernelT kern, size_t bytes) {
 
 }  // namespace
 
+// Frees the df-bound tables of device `dev` (stater_release_cache).
+void df_tables_release(int dev) {
+    std::lock_guard<std::mutex> lk(g_df_mutex);
+    for (auto it = g_df_tables.begin(); it != g_df_tables.end();) {
+        if (it->first.first == dev) {
+            cudaFree(it->second.lo);
+            cudaFree(it->second.hi);
+            it = g_df_tables.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
+
 stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s) {
     FastVars P;
     P.W = a->width;

@@ -146,9 +146,9 @@ constexpr int kLSB = STATER_LEV_SAMPLES_PER_STAGE;  // samples per stage (divide
 constexpr int kLStages = STATER_LEV_STAGES;
 
 template <int G, int QLO, int QHI>
-__device__ __forceinline__ bool lev_tma_consume(const float *stages, int stage_floats, uint64_t *full, uint64_t *empty,
-                                                int nchunks, int cnt, float &n, float (&piv)[G + 3], float *hi,
-                                                float *lo, int lane) {
+__device__ __forceinline__ bool lev_tma_consume(uint32_t wait_limit, const float *stages, int stage_floats,
+                                                uint64_t *full, uint64_t *empty, int nchunks, int cnt, float &n,
+                                                float (&piv)[G + 3], float *hi, float *lo, int lane) {
     using namespace tma;
     constexpr int P0 = G + 3;
     constexpr int NQ = QHI - QLO;
@@ -159,7 +159,7 @@ __device__ __forceinline__ bool lev_tma_consume(const float *stages, int stage_f
     for (int q = 0; q < NQ; q++) part[q] = 0.f;
     for (int c = 0; c < nchunks; c++) {
         const int sidx = c % kLStages;
-        if (!mbar_wait(&full[sidx], (c / kLStages) & 1)) return false;
+        if (!mbar_wait(&full[sidx], (c / kLStages) & 1, wait_limit)) return false;
         const float *rgb = stages + (size_t)sidx * stage_floats;  // [kLSB][3][kPx]
         const float *feat = rgb + kLSB * 3 * kPx;                 // [kLSB][G][kPx]
         const int jn = min(kLSB, cnt - c * kLSB);
@@ -221,6 +221,8 @@ struct LevTmaParams {
     const int32_t *count;
     float *state;
     int *err;
+    uint32_t wait_limit;  // polls of a pipeline wait
+    int stall;            // 1: the producer issues nothing (test hook: the consumers' waits run out)
 };
 
 template <int G>
@@ -267,9 +269,9 @@ __global__ void __launch_bounds__(kPx *(kParts + 1))
             const uint32_t bytes = (uint32_t)stage_floats * 4u;
             int issued = 0;
             bool ok = true;
-            for (int c = 0; c < nchunks && ok; c++) {
+            for (int c = 0; c < nchunks && ok && !LP.stall; c++) {
                 const int st = c % kLStages;
-                if (c >= kLStages) ok = mbar_wait(&empty[st], ((c / kLStages) - 1) & 1);
+                if (c >= kLStages) ok = mbar_wait(&empty[st], ((c / kLStages) - 1) & 1, LP.wait_limit);
                 if (!ok) break;
                 mbar_arrive_expect_tx(&full[st], bytes);
                 float *dst = stages + (size_t)st * stage_floats;
@@ -277,10 +279,13 @@ __global__ void __launch_bounds__(kPx *(kParts + 1))
                 if (G > 0) tma_load_3d(dst + kLSB * 3 * kPx, &map_feat, (int)p0, 5, c * kLSB, &full[st]);
                 issued = c + 1;
             }
-            if (!ok) {
-                atomicExch(LP.err, kErrTimeout);
-                for (int c = max(0, issued - kLStages); c < issued; c++) mbar_wait(&full[c % kLStages], (c / kLStages) & 1);
-            }
+            if (!ok) atomicOr(LP.err, kErrTimeout);
+            // the last boxes issued must have landed before the CTA may end (on
+            // success too: consumers that gave up may already have left)
+            bool drained = true;
+            for (int c = max(0, issued - kLStages); c < issued; c++)
+                drained = mbar_wait(&full[c % kLStages], (c / kLStages) & 1) && drained;
+            if (!drained) atomicOr(LP.err, kErrDrain);
         }
         return;
     }
@@ -300,13 +305,13 @@ __global__ void __launch_bounds__(kPx *(kParts + 1))
     const int cnt = valid ? (LP.count ? min(max(LP.count[p], 0), LP.S) : LP.S) : 0;
     bool ok;
     switch (J) {
-        case 0: ok = lev_tma_consume<G, 0, (QP < NSUM ? QP : NSUM)>(stages, stage_floats, full, empty, nchunks, cnt, n, piv, hi, lo, lane); break;
-        case 1: ok = lev_tma_consume<G, (QP < NSUM ? QP : NSUM), (2 * QP < NSUM ? 2 * QP : NSUM)>(stages, stage_floats, full, empty, nchunks, cnt, n, piv, hi, lo, lane); break;
-        case 2: ok = lev_tma_consume<G, (2 * QP < NSUM ? 2 * QP : NSUM), (3 * QP < NSUM ? 3 * QP : NSUM)>(stages, stage_floats, full, empty, nchunks, cnt, n, piv, hi, lo, lane); break;
-        default: ok = lev_tma_consume<G, (3 * QP < NSUM ? 3 * QP : NSUM), NSUM>(stages, stage_floats, full, empty, nchunks, cnt, n, piv, hi, lo, lane);
+        case 0: ok = lev_tma_consume<G, 0, (QP < NSUM ? QP : NSUM)>(LP.wait_limit, stages, stage_floats, full, empty, nchunks, cnt, n, piv, hi, lo, lane); break;
+        case 1: ok = lev_tma_consume<G, (QP < NSUM ? QP : NSUM), (2 * QP < NSUM ? 2 * QP : NSUM)>(LP.wait_limit, stages, stage_floats, full, empty, nchunks, cnt, n, piv, hi, lo, lane); break;
+        case 2: ok = lev_tma_consume<G, (2 * QP < NSUM ? 2 * QP : NSUM), (3 * QP < NSUM ? 3 * QP : NSUM)>(LP.wait_limit, stages, stage_floats, full, empty, nchunks, cnt, n, piv, hi, lo, lane); break;
+        default: ok = lev_tma_consume<G, (3 * QP < NSUM ? 3 * QP : NSUM), NSUM>(LP.wait_limit, stages, stage_floats, full, empty, nchunks, cnt, n, piv, hi, lo, lane);
     }
     if (!ok) {
-        if (lane == 0) atomicExch(LP.err, kErrTimeout);
+        if (lane == 0) atomicOr(LP.err, kErrTimeout);
         return;
     }
     if (!valid) return;
@@ -333,7 +338,7 @@ cudaError_t run_tma_g(size_t HW, int S, const float *samples, const int32_t *cou
     if (G > 0 && !encode_tensor_map_3d_f32(&mfeat, samples, HW, NCH, (uint64_t)S, kPx, G, kLSB))
         return cudaErrorNotSupported;
     if (G == 0) mfeat = mrgb;
-    LevTmaParams LP{HW, S, count, state, device_error_word()};
+    LevTmaParams LP{HW, S, count, state, device_error_word(), pipeline_wait_limit(), pipeline_stall()};
     if (!LP.err) return cudaErrorMemoryAllocation;
     const size_t smem = sizeof(float) * ((size_t)kLStages * kLSB * (3 + G) * kPx + 2 * (size_t)lev_part(G) * kPx * kParts);
     cudaError_t e = cudaFuncSetAttribute(lev_tma_f32<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

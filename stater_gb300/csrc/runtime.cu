@@ -3,6 +3,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <map>
@@ -12,9 +13,13 @@
 #include <vector>
 
 #include "common.cuh"
+#include "tma_common.cuh"
 #include "tquantile.h"
 
 namespace stater {
+
+void noalloc_forget_device(int dev);  // target_spp.cu
+void df_tables_release(int dev);      // denoise_fast.cu
 
 namespace {
 thread_local std::string g_last_error;
@@ -39,6 +44,11 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 EncodeTiledFn g_encode = nullptr;
+
+// Pipeline-wait settings of the TMA-fed kernels (stater_debug_set_pipeline_waits).
+std::atomic<uint32_t> g_wait_limit{tma::kWaitLimit};
+std::atomic<int> g_stall{0};
+constexpr uint32_t kStallMaxPolls = 1u << 16;
 
 constexpr int kLutIntervals = 1024;
 }  // namespace
@@ -96,6 +106,9 @@ void *scratch(int slot, size_t bytes, cudaStream_t stream) {
 }
 
 int tcrit_intervals() { return kLutIntervals; }
+
+uint32_t pipeline_wait_limit() { return g_wait_limit.load(); }
+int pipeline_stall() { return g_stall.load(); }
 
 // One int per device that kernels set when a bounded wait gives up.
 int *device_error_word() {
@@ -219,6 +232,10 @@ stater_status stater_synchronize(stater_stream stream) {
         if (e != cudaSuccess) return cuda_status(e, "stater_synchronize: error word");
         if (v != 0) {
             cudaMemset(w, 0, sizeof(int));
+            if (v & tma::kErrDrain)
+                return set_error(STATER_ERR_TIMEOUT,
+                                 "a bounded device wait gave up and so did the final wait for the copies in flight: "
+                                 "the pipeline is lost and the affected call's results are undefined");
             return set_error(STATER_ERR_TIMEOUT, "a bounded device wait gave up (pipeline stalled); results of the "
                                                  "affected call are incomplete");
         }
@@ -269,6 +286,23 @@ stater_status stater_release_cache(void) {
             ++it;
         }
     }
+    noalloc_forget_device(dev);
+    df_tables_release(dev);
+    return STATER_OK;
+}
+
+stater_status stater_debug_set_pipeline_waits(uint32_t wait_polls, int32_t stall_producers) {
+    clear_error();
+    const uint32_t limit = wait_polls == 0 ? tma::kWaitLimit : wait_polls;
+    if (limit > tma::kWaitLimit)
+        return set_error(STATER_ERR_INVALID, "stater_debug_set_pipeline_waits: more polls than the default limit");
+    if (stall_producers != 0 && stall_producers != 1)
+        return set_error(STATER_ERR_INVALID, "stater_debug_set_pipeline_waits: stall_producers must be 0 or 1");
+    if (stall_producers && limit > kStallMaxPolls)
+        return set_error(STATER_ERR_INVALID, "stater_debug_set_pipeline_waits: a stall needs a wait limit of at most "
+                                             "65536 polls");
+    g_wait_limit.store(limit);
+    g_stall.store(stall_producers);
     return STATER_OK;
 }
 

@@ -150,6 +150,15 @@ std::mutex g_noalloc_mutex;
 double *g_noalloc_ptr[64] = {nullptr};
 
 }  // namespace
+
+// Forgets the cached address of the array on device `dev` (stater_release_cache):
+// after a device reset the module is loaded again, possibly elsewhere, so the
+// next call must look the address up afresh.
+void noalloc_forget_device(int dev) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+    if (dev >= 0 && dev < 64) g_noalloc_ptr[dev] = nullptr;
+}
+
 }  // namespace stater
 
 extern "C" stater_status stater_calc_target_spp_noalloc(int32_t width, int32_t height, int32_t spp,

@@ -1,8 +1,13 @@
 // Inline-PTX helpers for the TMA-fed kernels: mbarrier init / arrive /
 // bounded wait, and tiled tensor loads (cp.async.bulk.tensor) that complete on
-// an mbarrier. Every wait is bounded by kWaitLimit polls; a wait that gives up
-// returns false and the kernel records kErrTimeout in the library's device
-// error word (reported by stater_synchronize).
+// an mbarrier. Every wait is bounded: the pipeline waits (consumers for a full
+// stage, the producer for a free one) by the limit the kernel is given
+// (kWaitLimit polls unless stater_debug_set_pipeline_waits lowered it), the
+// producer's final wait for the copies it issued always by kWaitLimit. A
+// pipeline wait that gives up returns false and the kernel ORs kErrTimeout into
+// the library's device error word; a final wait that gives up ORs kErrDrain
+// (copies may still have been in flight when the CTA ended). stater_synchronize
+// reports either as STATER_ERR_TIMEOUT.
 #pragma once
 
 #include <cuda.h>
@@ -11,6 +16,10 @@
 namespace stater {
 
 int *device_error_word();
+// Pipeline-wait limit and producer stall flag of the TMA-fed kernels
+// (stater_debug_set_pipeline_waits; defaults kWaitLimit and 0).
+uint32_t pipeline_wait_limit();
+int pipeline_stall();
 bool encode_tensor_map_2d_f32(CUtensorMap *map, const void *base, uint64_t cols, uint64_t rows, uint32_t box_cols,
                               uint32_t box_rows);
 // 3-D float tensor [d2][d1][d0] (d0 contiguous), box {b0, b1, b2}.
@@ -21,6 +30,7 @@ namespace tma {
 
 constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr int kErrTimeout = 1;
+constexpr int kErrDrain = 2;
 
 static __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -40,9 +50,9 @@ static __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint
                  : "memory");
 }
 
-// Bounded wait for the phase with parity `parity` to complete.
-static __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitLimit; i++) {
+// Bounded wait (at most `limit` polls) for the phase with parity `parity` to complete.
+static __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit = kWaitLimit) {
+    for (uint32_t i = 0; i < limit; i++) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"

@@ -6,8 +6,8 @@ with the lines they came from in film_constants.json next to this script. The
 oracle's film restatement is checked against that fixture, which pins the
 constants of Film::UpdateImage's XYZ round trip and of the luminance clamp.
 
-Needs the reference tree (STATER_REFERENCE, default /root/reference); run from the
-repository root:  python tests/golden/make_film_constants.py
+Needs the reference tree, named by STATER_REFERENCE; run from the repository root:
+    STATER_REFERENCE=<StatER tree> python tests/golden/make_film_constants.py
 """
 from __future__ import annotations
 
@@ -17,7 +17,7 @@ import re
 from pathlib import Path
 
 OUT = Path(__file__).resolve().parent / "film_constants.json"
-REF = Path(os.environ.get("STATER_REFERENCE", "/root/reference"))
+REF = Path(os.environ.get("STATER_REFERENCE", ""))
 
 
 def body(lines, signature):
@@ -43,6 +43,8 @@ def literals(text):
 
 
 def main():
+    if not str(REF) or not (REF / "src" / "core" / "spectrum.h").exists():
+        raise SystemExit("set STATER_REFERENCE to the StatER tree (src/core/spectrum.h not found)")
     src = REF / "src" / "core" / "spectrum.h"
     lines = src.read_text().splitlines(keepends=True)
     out = {"source": "src/core/spectrum.h"}

@@ -6,8 +6,10 @@ synthetic samples, the way StatPathIntegrator feeds it (16x16 tiles, two render
 iterations with persistent tile state, the second with uneven per-pixel sample
 counts), and stores inputs and outputs as .npz fixtures next to this script.
 
-Needs the reference tree (STATER_REFERENCE, default /root/reference); run from the
-repository root:  python tests/golden/make_golden.py
+Needs oracle/_ref, which oracle/build_ref.sh compiles from the reference tree
+named by STATER_REFERENCE; run from the repository root:
+    STATER_REFERENCE=<StatER tree> bash oracle/build_ref.sh
+    python tests/golden/make_golden.py
 """
 from __future__ import annotations
 

@@ -101,3 +101,13 @@ def test_job_footprint_grows_with_the_job(lib):
     assert f64 > small
     # 1080p, K=5, 32-spp chunk: about 1 GB of statistics/outputs plus a 3.2 GB sample chunk
     assert 3e9 < large < 6e9
+
+
+def test_pipeline_wait_hook_rejects(lib):
+    """The wait hook refuses limits above the default and stalls with long waits."""
+    assert lib.stater_debug_set_pipeline_waits((1 << 22) + 1, 0) == INVALID
+    assert lib.stater_debug_set_pipeline_waits(1 << 20, 1) == INVALID
+    assert b"65536" in lib.stater_last_error()
+    assert lib.stater_debug_set_pipeline_waits(100, 2) == INVALID
+    assert lib.stater_debug_set_pipeline_waits(256, 0) == 0
+    assert lib.stater_debug_set_pipeline_waits(0, 0) == 0

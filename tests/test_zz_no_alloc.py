@@ -40,16 +40,45 @@ def lib():
     return S.load()
 
 
+def _compare(lib, H, W, n, varD, mean):
+    ref = torch.zeros(H, W, dtype=torch.int32, device="cuda")
+    got = torch.full((H, W), -7, dtype=torch.int32, device="cuda")
+    assert _call(lib, "stater_calc_target_spp", W, H, n, varD, mean, ref) == 0
+    assert _call(lib, "stater_calc_target_spp_noalloc", W, H, n, varD, mean, got) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(got, ref), (H, W)
+
+
 def test_noalloc_matches_allocating_entry_point_twice_in_a_row(lib):
-    for (H, W, seed, relative) in ((1080, 1920, 1, True), (301, 517, 2, False)):
+    # 1080p, a ragged size, exactly the limit (2048 x 1024 = 2^21 pixels: the
+    # errors fill the whole array and the deepest reduction runs) and a single
+    # pixel (no reduction level, the one-value copy)
+    for (H, W, seed, relative) in ((1080, 1920, 1, True), (301, 517, 2, False), (1024, 2048, 5, True),
+                                   (1, 1, 6, True), (1, 1, 7, False)):
         n, varD, mean = _inputs(H, W, seed)
-        m = mean if relative else None
-        ref = torch.zeros(H, W, dtype=torch.int32, device="cuda")
-        got = torch.full((H, W), -7, dtype=torch.int32, device="cuda")
-        assert _call(lib, "stater_calc_target_spp", W, H, n, varD, m, ref) == 0
-        assert _call(lib, "stater_calc_target_spp_noalloc", W, H, n, varD, m, got) == 0
-        torch.cuda.synchronize()
-        assert torch.equal(got, ref)
+        if H * W == 1:
+            n.fill_(40)
+        _compare(lib, H, W, n, varD, mean if relative else None)
+
+
+def test_noalloc_pixels_without_statistics(lib):
+    # no pixel has two samples: every target is the maximum, the sum of errors is 0
+    n, varD, mean = _inputs(37, 53, 8)
+    n.fill_(1)
+    n[5, 5] = 0
+    _compare(lib, 37, 53, n, varD, mean)
+    # a mix in which every valid pixel has zero variance: total 0, targets = spp
+    n, varD, mean = _inputs(37, 53, 9)
+    varD.zero_()
+    _compare(lib, 37, 53, n, varD, None)
+
+
+def test_noalloc_after_release_cache(lib):
+    # stater_release_cache forgets the array's address; the next call looks it up again
+    n, varD, mean = _inputs(64, 96, 10)
+    _compare(lib, 64, 96, n, varD, mean)
+    assert lib.stater_release_cache() == 0
+    _compare(lib, 64, 96, n, varD, mean)
 
 
 def test_noalloc_f32_inputs(lib):
