@@ -208,6 +208,52 @@ def hbm_peak_gbs():
         return 6800.0, "fallback"
 
 
+def fp32_peak_tflops(S, reps=5):
+    """FP32 rate of this GPU with its own FMA instructions (stater_fp32_peak_probe:
+    8 independent chains per thread, scalar fma.rn.f32 and packed fma.rn.f32x2),
+    timed with CUDA events; the larger of the two medians, in TFLOP/s."""
+    import ctypes as C
+
+    import torch
+    lib = S.load()
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    blocks = props.multi_processor_count * 8
+    sink = torch.zeros(blocks, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    out = {}
+    for packed in (0, 1):
+        flops = C.c_double(0.0)
+        ms = []
+        for i in range(reps + 2):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rc = lib.stater_fp32_peak_probe(blocks, 2048, packed, C.c_void_p(sink.data_ptr()), C.byref(flops),
+                                            C.c_void_p(stream.cuda_stream))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if rc != 0:
+                raise RuntimeError("stater_fp32_peak_probe failed")
+            if i >= 2:
+                ms.append(e0.elapsed_time(e1))
+        out["packed" if packed else "scalar"] = flops.value / (statistics.median(ms) / 1e3) / 1e12
+    return max(out.values()), out
+
+
+# Algorithmic FP32 operations per (pixel, in-window neighbour) of the two
+# window filters at the benchmark's configuration (an FMA counts 2, a compare
+# or exp2 1). Range weight: spatial term 2 + 3 per feature channel (difference,
+# FMA) + exp2 1. Variance filter, per transform and channel: log-variance
+# difference 1, threshold FMA 2, compare 1, weight sum 1, weighted variance FMA
+# 2. Film filter, per transform and channel: mean difference 1, summed variance
+# 1, square 1, the two df-bound products 2, two compares 2; plus the film sums,
+# 4 FMAs. The film filter's count is the formula's (every transform tested for
+# every neighbour); the kernel stops at the first rejecting transform, so it
+# executes fewer.
+def filter_flops_per_pair(K, G):
+    weight = 2 + 3 * G + 1
+    return {"vars": weight + K * 3 * 7, "film": weight + K * 3 * 7 + 8}
+
+
 def max_over_ranks(ms, world, dist, device="cuda"):
     """The largest of the ranks' timings: the job is as slow as its slowest replica."""
     import torch
@@ -220,8 +266,12 @@ def max_over_ranks(ms, world, dist, device="cuda"):
 
 def accuracy_vs_plain(S, b, film, pb, pfilm):
     """Error of the FP32 form against the plain FP64 form on the same samples:
-    relative error of filmD (to each pixel's largest channel) and the fraction of
-    Welch accept/reject decisions (pixel x neighbour x transform) that differ."""
+    the fraction of Welch accept/reject decisions (pixel x neighbour x transform)
+    that differ; the relative error of filmD (per channel) at its maximum over
+    the pixels whose window has no flipped decision in any transform (both forms
+    average the same neighbours there), the fraction of pixels with a flip and
+    the maximum over them; and, for reference, the error relative to each
+    pixel's largest channel over all pixels."""
     import torch
     w = WORKLOAD
     R = w["radius"]
@@ -243,15 +293,23 @@ def accuracy_vs_plain(S, b, film, pb, pfilm):
     v = (v + (v >> 4)) & 0x0F0F0F0F
     v = (v & 0xFF) + ((v >> 8) & 0xFF) + ((v >> 16) & 0xFF) + ((v >> 24) & 0xFF)
     flips = int(v.sum(dtype=torch.int64).item())
+    flipped = ((bits[0] ^ bits[1]) != 0).any(dim=2).any(dim=1)  # [HW]: some decision of the pixel differs
     total = b.H * b.W * K * (2 * R + 1) ** 2
     a = b.filmD.double()
     r = pb.filmD.double()
+    rel_ch = ((a - r).abs() / r.abs().clamp_min(1e-12)).amax(dim=0).flatten()
+    clean = rel_ch[~flipped]
+    dirty = rel_ch[flipped]
     scale = r.abs().amax(dim=0, keepdim=True).clamp_min(1e-30)
     rel = ((a - r).abs() / scale).flatten()
     q = float(torch.quantile(rel[torch.randperm(rel.numel(), device=rel.device)[:1 << 20]], 0.999).item())
     del bits, v
-    return {"filmD_rel_max": float(rel.max().item()), "filmD_rel_p999": q,
-            "flipped_decisions": flips / total, "decisions": total}
+    return {"filmD_rel_max_unflipped": float(clean.max().item()) if clean.numel() else 0.0,
+            "pixels_with_flip_frac": float(flipped.double().mean().item()),
+            "filmD_rel_max_flipped": float(dirty.max().item()) if dirty.numel() else 0.0,
+            "filmD_rel_max": float(rel.max().item()), "filmD_rel_p999": q,
+            "flipped_decisions": flips / total, "decisions": total,
+            "comparator": "plain FP64 GPU form (pinned to the FP64 oracle at 256x256, same transforms and window)"}
 
 
 def run_gpu(args, rank, world, dist):
@@ -341,10 +399,34 @@ def run_gpu(args, rank, world, dist):
                 "algorithmic_gb": acc_bytes / 1e9,
                 "peak_source": peak_source}
 
+    # roofline of the two window filters: FP32 ALU work against the FP32 rate
+    # measured here with the library's FMA probe
+    fp32_peak, fp32_forms = fp32_peak_tflops(S)
+    R = w["radius"]
+    pairs = HW * (2 * R + 1) ** 2  # interior count; border pixels have fewer neighbours
+    fpp = filter_flops_per_pair(K, G)
+    roofline_filters = {"bound": "fp32", "unit": "TFLOP/s", "peak": fp32_peak,
+                        "peak_source": "stater_fp32_peak_probe in this run (FMA chains; scalar "
+                                       f"{fp32_forms['scalar']:.1f}, packed {fp32_forms['packed']:.1f} TFLOP/s)"}
+    for name, stage, kern in (("vars", "denoise_vars", "vars_stats_f32 + vars_ring_f32"),
+                              ("film", "denoise_film", "film_discr_f32 + film_ring_f32")):
+        ms_ = statistics.median(stage_ms[stage])
+        ach = pairs * fpp[name] / (ms_ / 1e3) / 1e12
+        roofline_filters[name] = {"kernel": kern, "flops_per_pixel": fpp[name] * (2 * R + 1) ** 2, "ms": ms_,
+                                  "achieved": ach, "frac": ach / fp32_peak}
+    # the variance filter's shared-memory traffic: per neighbour, the feature
+    # record (2 x 16 B) and two 16-byte records per transform, over the SMs'
+    # 128 B/clock at the sampled SM clock
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    sm_mhz = clk.summary().get("sm_mhz") or 2070.0
+    smem_bytes = pairs * (2 + 2 * K) * 16
+    roofline_filters["vars"]["smem_frac"] = smem_bytes / (statistics.median(stage_ms["denoise_vars"]) / 1e3) / (
+        props.multi_processor_count * 128 * sm_mhz * 1e6)
+
     del samples
     torch.cuda.empty_cache()
 
-    extra = {}
+    extra = {"roofline_filters": roofline_filters}
     # plain FP64 form (one image per launch), same workload
     if not args.no_plain:
         pb = S.StatBuffers(W, H, w["transforms"], G, w["max_moment"], S.F64)

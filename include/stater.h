@@ -120,6 +120,14 @@ int32_t stater_abi_version(void);
  * it has issued always keeps the default limit. Settings are process-wide and
  * apply to launches made after the call. */
 stater_status stater_debug_set_pipeline_waits(uint32_t wait_polls, int32_t stall_producers);
+/* FP32 throughput probe, no counterpart in the reference: launches `blocks`
+ * CTAs of 256 threads, each thread running 8 independent chains of 16 * iters
+ * FMAs (packed = 1: fma.rn.f32x2, two lanes per instruction), and returns in
+ * *flops the floating-point operations launched (an FMA counts 2). Timing the
+ * launch gives the FP32 rate the stage-2 filters are measured against. sink:
+ * device float [blocks], written only if a chain reaches an impossible value. */
+stater_status stater_fp32_peak_probe(int32_t blocks, int32_t iters, int32_t packed, float *sink, double *flops,
+                                     stater_stream stream);
 /* Releases cached device scratch and tables of the current device and forgets
  * the cached device addresses of the library's fixed arrays. Call it before a
  * device reset (cudaDeviceReset) that is followed by further calls into the

@@ -109,6 +109,7 @@ def load() -> C.CDLL:
         "stater_abi_version": (C.c_int32, []),
         "stater_release_cache": (st, []),
         "stater_debug_set_pipeline_waits": (st, [C.c_uint32, C.c_int32]),
+        "stater_fp32_peak_probe": (st, [C.c_int32, C.c_int32, C.c_int32, VP, C.POINTER(C.c_double), VP]),
         "stater_accumulate": (st, [C.POINTER(AccumulateArgs), VP]),
         "stater_generate_samples": (st, [C.POINTER(GenerateArgs), VP]),
         "stater_merge_tiles": (st, [C.c_int32, C.c_int32, C.c_int32, VP, VP, C.c_int32, VP, VP, VP]),

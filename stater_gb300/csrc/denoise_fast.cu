@@ -836,7 +836,19 @@ __device__ __forceinline__ float4 film_ring_value(const FastFilm &P, int rec, in
     return v;
 }
 
-template <int KMAX, int TY>
+// The film filter in two passes per window row. Pass A tests, for all 2R + 1
+// neighbours of the row in lockstep, only the upper df bound of the first
+// transform in test order (the JB choice in STATER_MT_JB mode): a neighbour it
+// rejects is rejected by the full test too, and on the benchmark's radiance it
+// rejects most of them. Each lane keeps the survivors as bits of a 64-bit mask.
+// Pass B walks each lane's own survivors in increasing dx and runs the full
+// test (every transform in test order, the exact df only in the band between
+// the bounds) and, for accepted ones, the range weight and the film sums.
+// Lanes therefore no longer idle while a neighbour of another lane goes through
+// all transforms, and every pixel still sums its accepted neighbours in the
+// same order (rows, then dx), so filmD is bitwise that of the per-transform
+// kernel.
+template <int KMAX, int TY, bool JB>
 __global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
     constexpr int NS = TY + 1;
     extern __shared__ float4 ring[];
@@ -883,7 +895,7 @@ __global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
     const bool act = in && ni >= 2;
     // slots hold the transforms in test order; ksel is the slot of the JB choice
     int ksel = -1;
-    if (act && P.mt_mode == STATER_MT_JB) {
+    if (JB && act) {
         int kbest = 0;
         float best = __ldg(P.jb[0] + gi);
         for (int k = 1; k < K; k++) {
@@ -910,6 +922,22 @@ __global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
             mi[sl][c] = ok ? __ldg(mean + (size_t)c * HW + gi) : 0.f;
             di[sl][c] = ok ? __ldg(P.discr[k] + (size_t)c * HW + gi) : 0.f;
         }
+    // the slot pass A tests and its centre values
+    const int slotA = JB ? max(ksel, 0) : 0;
+    float mA[3], dA[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        mA[c] = mi[0][c];
+        dA[c] = di[0][c];
+        if (JB) {
+#pragma unroll
+            for (int sl = 1; sl < KMAX; sl++)
+                if (sl == slotA) {
+                    mA[c] = mi[sl][c];
+                    dA[c] = di[sl][c];
+                }
+        }
+    }
     __syncthreads();
     const bool uni = s_nmin == s_nmax;
     float tlo_u = 0.f, thi_u = 0.f;
@@ -918,6 +946,16 @@ __global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
         tlo_u = dfl > kDfMax ? P.z2lo : __ldg(P.tlo + dfl);
         thi_u = __ldg(P.thi + (dfh > kDfMax ? kDfMax : dfh));
     }
+    auto bounds = [&](int nj, float &tlo, float &thi) {
+        tlo = tlo_u;
+        thi = thi_u;
+        if (!uni) {
+            const int njc = max(nj, 2);
+            const int dfl = ni + njc - 2, dfh = min(ni, njc) - 1;
+            tlo = dfl > kDfMax ? P.z2lo : __ldg(P.tlo + dfl);
+            thi = __ldg(P.thi + (dfh > kDfMax ? kDfMax : dfh));
+        }
+    };
 
     float sw = 0.f, sf[3] = {0.f, 0.f, 0.f};
     for (int r = -R; r <= R; r++) {
@@ -930,22 +968,43 @@ __global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
         }
         if (act) {
             const float4 *rp = ring + (size_t)((tr + R + r) % NS) * nrec * hw + lx + R;
+            // pass A: the upper-bound test of slot A for every neighbour of the row
+            uint64_t cand = 0;
+            {
+                const float4 *ap = rp + (size_t)(kRingFW + 1 + 2 * slotA) * hw;
+                for (int dx = -R; dx <= R; dx++) {
+                    float thi = thi_u;
+                    if (!uni) {
+                        float tlo;
+                        bounds((int)rp[hw + dx].w, tlo, thi);
+                    }
+                    const float4 T0 = ap[dx], T1 = ap[hw + dx];
+                    const float mj[3] = {T0.x, T0.y, T0.z}, dj[3] = {T0.w, T1.x, T1.y};
+                    bool hi = true;
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float diff = mA[c] - mj[c];
+                        const float sv = dA[c] + dj[c];
+                        hi = hi && diff * diff <= thi * sv;
+                    }
+                    cand |= (uint64_t)hi << (dx + R);
+                }
+            }
+            if (r == 0) cand |= 1ull << R;  // the centre is always kept
+            // pass B: the lane's survivors, in increasing dx
             const float sdy = P.ds2 * (float)(r * r);
-            for (int dx = -R; dx <= R; dx++) {
+            while (cand) {
+                const int dx = __ffsll((long long)cand) - 1 - R;
+                cand &= cand - 1;
                 const float4 F1 = rp[hw + dx];
                 const int nj = (int)F1.w;
                 bool a = nj >= 2;
-                float tlo = tlo_u, thi = thi_u;
-                if (!uni) {
-                    const int njc = max(nj, 2);
-                    const int dfl = ni + njc - 2, dfh = min(ni, njc) - 1;
-                    tlo = dfl > kDfMax ? P.z2lo : __ldg(P.tlo + dfl);
-                    thi = __ldg(P.thi + (dfh > kDfMax ? kDfMax : dfh));
-                }
+                float tlo, thi;
+                bounds(nj, tlo, thi);
 #pragma unroll
                 for (int k = 0; k < KMAX; k++) {
                     if (k >= K) break;
-                    if (!a || (ksel >= 0 && ksel != k)) continue;
+                    if (!a || (JB && ksel != k)) continue;
                     const float4 *tp = rp + (size_t)(kRingFW + 1 + 2 * k) * hw + dx;
                     const float4 T0 = tp[0], T1 = tp[hw];
                     const float mj[3] = {T0.x, T0.y, T0.z}, dj[3] = {T0.w, T1.x, T1.y};
@@ -954,10 +1013,10 @@ __global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         const float diff = mi[k][c] - mj[c];
-                        const float s = di[k][c] + dj[c];
+                        const float sv = di[k][c] + dj[c];
                         const float qq = diff * diff;
-                        const bool lo = qq <= tlo * s;
-                        const bool hi = qq <= thi * s;
+                        const bool lo = qq <= tlo * sv;
+                        const bool hi = qq <= thi * sv;
                         acc = acc && hi;
                         amb = amb || (hi && !lo);
                     }
@@ -965,9 +1024,9 @@ __global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
 #pragma unroll
                         for (int c = 0; c < 3; c++) {
                             const float diff = mi[k][c] - mj[c];
-                            const float s = di[k][c] + dj[c];
+                            const float sv = di[k][c] + dj[c];
                             const float qq = diff * diff;
-                            if (!(qq <= tlo * s) && qq <= thi * s)
+                            if (!(qq <= tlo * sv) && qq <= thi * sv)
                                 acc = acc && welch_exact(diff, di[k][c], dj[c], ni, nj, P.lut, P.lut_n);
                         }
                     }
@@ -1262,13 +1321,16 @@ stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s
             const size_t sm = ring_smem(P.R, nrec, ty);
             dim3 grid((P.W + kTX2 - 1) / kTX2, (P.H + ty - 1) / ty);
             cudaError_t e = cudaErrorInvalidValue;
-#define STATER_RING_FILM(KV, TV)                                                   \
-    if (km == KV && ty == TV) {                                                     \
-        e = set_smem(film_ring_f32<KV, TV>, sm);                                    \
-        if (e == cudaSuccess) film_ring_f32<KV, TV><<<grid, kTX2 * TV, sm, s>>>(P); \
+            const bool jb = P.mt_mode == STATER_MT_JB;
+#define STATER_RING_FILM(KV, TV, JV)                                                          \
+    if (km == KV && ty == TV && jb == JV) {                                                    \
+        e = set_smem(film_ring_f32<KV, TV, JV>, sm);                                           \
+        if (e == cudaSuccess) film_ring_f32<KV, TV, JV><<<grid, kTX2 * TV, sm, s>>>(P);        \
     }
-            STATER_RING_FILM(1, 8) STATER_RING_FILM(3, 8) STATER_RING_FILM(5, 8)
-            STATER_RING_FILM(1, 4) STATER_RING_FILM(3, 4) STATER_RING_FILM(5, 4)
+            STATER_RING_FILM(1, 8, false) STATER_RING_FILM(3, 8, false) STATER_RING_FILM(5, 8, false)
+            STATER_RING_FILM(1, 4, false) STATER_RING_FILM(3, 4, false) STATER_RING_FILM(5, 4, false)
+            STATER_RING_FILM(1, 8, true) STATER_RING_FILM(3, 8, true) STATER_RING_FILM(5, 8, true)
+            STATER_RING_FILM(1, 4, true) STATER_RING_FILM(3, 4, true) STATER_RING_FILM(5, 4, true)
 #undef STATER_RING_FILM
             if (e != cudaSuccess) return cuda_status(e, "film_ring_f32 smem attribute");
             STATER_CHECK_LAUNCH("film_ring_f32");

@@ -43,3 +43,55 @@ def moment_scale(stats, n, q):
     nn = np.maximum(n, 1)[None, None]
     s = np.sqrt(m2 / nn)
     return nn * s ** q + 1e-300
+
+
+def decision_flips(bits_a, bits_b):
+    """Per-pixel flag: any Welch accept/reject decision (neighbour x transform)
+    differs between two accept-bit arrays [HW, K, words]."""
+    d = np.bitwise_xor(np.asarray(bits_a).view(np.uint32), np.asarray(bits_b).view(np.uint32))
+    return np.any(d != 0, axis=tuple(range(1, d.ndim)))
+
+
+def var_test_near_boundary(lnS2, se2, n, R, var_z, rel_margin=1e-3):
+    """Per-pixel flag [H, W]: some variance-test decision of the pixel (any
+    in-window neighbour with n >= 2, transform, channel) lies within rel_margin of
+    its threshold, (lnS2_i - lnS2_j)^2 vs z^2 (se2_i + se2_j), in the FP64
+    values given. Only there can a form whose inputs differ by ~1e-6 relative
+    decide otherwise; everywhere else both forms keep the same neighbours."""
+    lnS2 = np.asarray(lnS2, np.float64)
+    se2 = np.asarray(se2, np.float64)
+    K, C, H, W = lnS2.shape
+    z2 = float(var_z) ** 2
+    valid = np.asarray(n) >= 2
+    near = np.zeros((H, W), bool)
+    for dy in range(-R, R + 1):
+        yi = slice(max(0, -dy), min(H, H - dy))
+        yj = slice(max(0, dy), min(H, H + dy))
+        for dx in range(-R, R + 1):
+            if dx == 0 and dy == 0:
+                continue
+            xi = slice(max(0, -dx), min(W, W - dx))
+            xj = slice(max(0, dx), min(W, W + dx))
+            if yi.start >= yi.stop or xi.start >= xi.stop:
+                continue
+            dl = lnS2[..., yi, xi] - lnS2[..., yj, xj]
+            thr = z2 * (se2[..., yi, xi] + se2[..., yj, xj])
+            m = np.abs(dl * dl - thr) <= rel_margin * np.abs(thr)
+            m = np.any(m, axis=(0, 1)) & valid[yi, xi] & valid[yj, xj]
+            near[yi, xi] |= m
+    return near
+
+
+def split_rel_error(got, ref, flagged, floor=1e-12):
+    """Relative error |got - ref| / max(|ref|, floor) of [..., H, W] arrays split
+    by a per-pixel flag [H, W] (or [HW]): (max over unflagged pixels, max over
+    flagged pixels, fraction of pixels flagged)."""
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    rel = np.abs(got - ref) / np.maximum(np.abs(ref), floor)
+    rel = rel.reshape(-1, rel.shape[-2] * rel.shape[-1]).max(axis=0)
+    flagged = np.asarray(flagged).reshape(-1)
+    clean = rel[~flagged]
+    dirty = rel[flagged]
+    return (float(clean.max()) if clean.size else 0.0, float(dirty.max()) if dirty.size else 0.0,
+            float(flagged.mean()))

@@ -4,9 +4,11 @@ GPU, through properties that do not need the CPU oracle at this size:
 * accumulating the samples in four calls of 64 equals one call of 256, bit for
   bit (statistics, feature means, counts and film sums persist across calls);
 * every count and film weight equals 256;
-* the FP32 form against the plain FP64 form on the same samples: denoised film
-  within 1e-4 of each pixel's largest channel at the 99.9th percentile, and at
-  most 0.1% of the Welch accept/reject decisions flipped.
+* the FP32 form against the plain FP64 form on the same samples: at most 0.1%
+  of the Welch accept/reject decisions flipped, and the denoised film within
+  1e-4 (relative, per channel) at every pixel with no flipped decision in its
+  window. (The plain FP64 form itself is pinned against the FP64 oracle at
+  256x256 with the same transforms and window in test_gpu_configs.py.)
 """
 import pytest
 
@@ -76,9 +78,11 @@ def test_fp32_against_plain_fp64_full_size(S, samples):
         out.append((b.filmD.double(), bits))
         del b, film
     (a, ba), (r, br) = out
-    scale = r.abs().amax(dim=0, keepdim=True).clamp_min(1e-30)
-    rel = ((a - r).abs() / scale).flatten()
-    sample = rel[torch.randperm(rel.numel(), device=rel.device)[:1 << 22]]
-    assert float(torch.quantile(sample, 0.999)) <= 1e-4
-    flips = _popcount_sum(ba ^ br) / (H * W * len(TR) * (2 * R + 1) ** 2)
-    assert flips <= 1e-3
+    x = ba ^ br
+    flipped = (x != 0).any(dim=2).any(dim=1)  # [HW]
+    rel = ((a - r).abs() / r.abs().clamp_min(1e-12)).amax(dim=0).flatten()
+    clean_max = float(rel[~flipped].max().item())
+    flips = _popcount_sum(x) / (H * W * len(TR) * (2 * R + 1) ** 2)
+    assert flips <= 1e-3, flips
+    assert clean_max <= 1e-4, clean_max
+    assert float(flipped.double().mean().item()) <= 0.01
