@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define STATER_ABI_VERSION 1
+#define STATER_ABI_VERSION 2
 #define STATER_MAX_TRANSFORMS 8 /* buffers b0..b7 per statistics type */
 #define STATER_MAX_GBUFFERS 8
 #define STATER_MAX_FEATURES 16
@@ -74,6 +74,27 @@ typedef enum {
     STATER_MT_ALL = 2, /* neighbour kept only if every transform accepts it */
     STATER_MT_JB = 3   /* only the transform with the lowest Jarque-Bera score at the centre */
 } stater_mt_mode;
+
+/* Variance behind the Welch discriminator of denoiseFilm: the reference's
+ * CASCADE_MODE build switch (scripts/alternate-builds/build-asm+m.sh sets 0 for
+ * the "M" variant; MC and MCL keep the default 1). The cascade feeds the
+ * denoised variances of denoiseVars into the mean filter; without it, each pixel
+ * uses its own sample variance (denoiseVars is then needed only for adaptive
+ * sampling, as the comment in build-asm+m.sh notes). */
+typedef enum {
+    STATER_DISCR_DENOISED = 0, /* CASCADE_MODE=1: varCD with use_levc, else varD */
+    STATER_DISCR_SAMPLE = 1    /* CASCADE_MODE=0: m2C / (n - 1) with use_levc, else m2 / (n - 1) */
+} stater_discr_source;
+
+/* Variance behind the adaptive-sampling error estimate of calcTargetSPP: the
+ * reference's AS_MODE build switch ("ASM" by default, "ASN" with AS_MODE=0 in
+ * scripts/alternate-builds/build-asn+mcl.sh). calcTargetSPP receives both n, m2
+ * and varD (estimator.cpp:502-511); ASM uses the denoised variance, ASN the
+ * pixel's own sample variance m2 / (n - 1). */
+typedef enum {
+    STATER_AS_DENOISED = 0, /* "ASM", AS_MODE=1 */
+    STATER_AS_SAMPLE = 1    /* "ASN", AS_MODE=0 */
+} stater_as_source;
 
 typedef enum {
     STATER_ACC_EXACT = 0, /* the reference's operation order: x/n division, libm-accurate transforms */
@@ -290,8 +311,37 @@ typedef struct {
      * on the order). A permutation of 0..n_buffers-1, or all zero for the
      * reverse index order. stater_test_order gives one from the transform kinds. */
     int32_t test_order[STATER_MAX_TRANSFORMS];
+    /* stater_discr_source (0, the default, is the reference's default build) and
+     * the buffers STATER_DISCR_SAMPLE reads: m2 (moments) without use_levc, the
+     * m2C output of stater_denoise_vars with it. */
+    int32_t discr_source;
+    const void *m2[STATER_MAX_TRANSFORMS];
+    const void *m2C[STATER_MAX_TRANSFORMS];
 } stater_denoise_film_args;
 stater_status stater_denoise_film(const stater_denoise_film_args *a, stater_stream stream);
+
+/* The reference's own buffer layout (estimator.cpp:26-81): the Estimator owns
+ * pitched cv::cuda::GpuMat images and passes the denoiser PtrStepSzb tables
+ * {data, step, rows, cols}. An RGB buffer is one image of interleaved channels
+ * (CV_32FC3 with STATER_F32, CV_64FC3 with STATER_F64); n, jb and one-channel
+ * G-buffers are one-channel images. Element (c, x, y) of a buffer with C
+ * channels is at data + y * step + (x * C + c) * element size. The pitched entry
+ * points take the same argument blocks as the planar ones, with every buffer
+ * pointer naming the caller's pitched image (`data` of its PtrStepSzb), and one
+ * step per kind of buffer (cudaMallocPitch gives every image of the same row
+ * width the same pitch). accept_bits stays a plain array. Results equal the
+ * planar call's bit for bit. */
+typedef struct {
+    int64_t rgb_step;    /* bytes per row of every RGB buffer and 3-channel G-buffer (>= 3 W element size) */
+    int64_t scalar_step; /* bytes per row of jb and 1-channel G-buffers (>= W element size) */
+    int64_t n_step;      /* bytes per row of the int32 count image n (>= 4 W) */
+} stater_pitched_layout;
+/* stat_denoiser::denoiseVars<float3> over the layout above (estimator.cpp:374-414). */
+stater_status stater_denoise_vars_pitched(const stater_denoise_vars_args *a, const stater_pitched_layout *layout,
+                                          stater_stream stream);
+/* stat_denoiser::denoiseFilm over the layout above (estimator.cpp:421-457). */
+stater_status stater_denoise_film_pitched(const stater_denoise_film_args *a, const stater_pitched_layout *layout,
+                                          stater_stream stream);
 
 /* A test order for stater_denoise_film_args.test_order: the most compressing
  * transforms first (asinh, cbrt and Box-Cox with lambda < 1/2, sqrt, log1p,
@@ -316,6 +366,24 @@ stater_status stater_calc_target_spp(int32_t width, int32_t height, int32_t spp,
                                      const void *varD, const void *mean, double eps,
                                      int32_t tmin, int32_t tmax, int32_t *targetspp,
                                      stater_stream stream);
+
+/* calcTargetSPP with the reference's AS_MODE choice: as stater_calc_target_spp,
+ * but the per-pixel variance is varD (as_source STATER_AS_DENOISED, "ASM") or
+ * the sample variance m2 / (n - 1) (STATER_AS_SAMPLE, "ASN"); the buffer the
+ * choice does not read may be NULL. */
+typedef struct {
+    int32_t width, height, spp;
+    stater_precision precision;
+    const int32_t *n;
+    const void *m2;             /* RGB buffer, read by STATER_AS_SAMPLE */
+    const void *varD;           /* RGB buffer, read by STATER_AS_DENOISED */
+    const void *mean;           /* nullable: relative error (divide by mean^2 + eps) */
+    double eps;
+    int32_t tmin, tmax;
+    int32_t as_source;          /* stater_as_source */
+    int32_t *targetspp;
+} stater_target_spp_args;
+stater_status stater_calc_target_spp_ex(const stater_target_spp_args *a, stater_stream stream);
 
 /* No counterpart in the reference. The same computation as
  * stater_calc_target_spp for callers that cannot allocate device memory (pool

@@ -130,7 +130,10 @@ def tcrit2_table(alpha, N=1024):
 
 
 def denoise_film(n, stats, varD, varCD, jb, gmean, film, R, ds_factor, alpha, gspecs, mt_mode=MT_ALL,
-                 use_levc=False, want_bits=False, lut=None, nthreads=None):
+                 use_levc=False, want_bits=False, lut=None, nthreads=None, discr_source=0, m2C=None):
+    """discr_source 0: Welch discriminator from varCD (use_levc) or varD; 1 (the
+    reference's CASCADE_MODE=0): from m2C (use_levc; denoise_vars' output) or the
+    m2 moments, divided by n - 1."""
     lib = load()
     K, _, _, H, W = stats.shape
     if lut is None:
@@ -142,19 +145,24 @@ def denoise_film(n, stats, varD, varCD, jb, gmean, film, R, ds_factor, alpha, gs
     bits = np.zeros((H * W, K, words), np.uint32) if want_bits else None
     g, ng = gbufs(gspecs)
     lib.orc_denoise_film_f64(W, H, K, _p(_c(n, np.int32)), _p(_c(stats, np.float64)), _p(_c(varD, np.float64)),
-                             _p(_c(varCD, np.float64)), _p(_c(jb, np.float64)), int(use_levc), int(mt_mode), R,
+                             _p(_c(varCD, np.float64)), _p(_c(jb, np.float64)), int(use_levc), int(discr_source),
+                             _p(None if m2C is None else _c(m2C, np.float64)), int(mt_mode), R,
                              C.c_double(ds_factor), len(lut) - 1, _p(_c(lut, np.float64)), ng, g,
                              _p(_c(gmean, np.float64)), _p(_c(film, np.float64)), _p(discr), _p(filmD), _p(bits),
                              nthreads or threads())
     return {"discr": discr, "filmD": filmD, "bits": bits}
 
 
-def calc_target_spp(n, varD, mean, spp, eps=1e-4, tmin=16, tmax=1024):
+def calc_target_spp(n, varD, mean, spp, eps=1e-4, tmin=16, tmax=1024, m2=None, as_source=0):
+    """as_source 0 ("ASM"): from varD; 1 ("ASN"): from the sample variance m2 / (n - 1)."""
     lib = load()
     H, W = n.shape
     out = np.zeros((H, W), np.int32)
-    lib.orc_calc_target_spp(W, H, int(spp), _p(_c(n, np.int32)), _p(_c(varD, np.float64)),
-                            _p(None if mean is None else _c(mean, np.float64)), C.c_double(eps), tmin, tmax, _p(out))
+    lib.orc_calc_target_spp_src(W, H, int(spp), _p(_c(n, np.int32)),
+                                _p(None if varD is None else _c(varD, np.float64)),
+                                _p(None if m2 is None else _c(m2, np.float64)), int(as_source),
+                                _p(None if mean is None else _c(mean, np.float64)), C.c_double(eps), tmin, tmax,
+                                _p(out))
     return out
 
 

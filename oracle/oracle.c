@@ -470,9 +470,9 @@ void orc_denoise_vars_f64(int W, int H, int K, int max_moment, const int32_t *n,
 /* Stage 2c: Welch-discriminated mean filter (denoiseFilm).                   */
 /* ------------------------------------------------------------------------- */
 typedef struct {
-    int W, H, K, R, nG, use_levc, mt_mode, lut_n;
+    int W, H, K, R, nG, use_levc, discr_source, mt_mode, lut_n;
     const int32_t *n;
-    const double *stats, *varD, *varCD, *jb, *tcrit2, *gmean, *film;
+    const double *stats, *varD, *varCD, *m2C, *jb, *tcrit2, *gmean, *film;
     double ds_factor;
     const orc_gbuf *gbufs;
     double *discr, *filmD;
@@ -493,7 +493,16 @@ static void film_discr_range(void *vctx, int64_t b, int64_t e) {
                     c->ediv[o] = 0.0;
                     continue;
                 }
-                const double v = c->use_levc ? c->varCD[o] : c->varD[o];
+                /* the reference's CASCADE_MODE: denoised variance (1, default) or the
+                 * pixel's own sample variance (0, the "M" build) */
+                double v;
+                if (c->discr_source == 1) {
+                    const double m2 = c->use_levc ? c->m2C[o]
+                                                  : c->stats[((size_t)(k * ORC_NQ + ORC_Q_M2) * 3 + ch) * HW + p];
+                    v = m2 / (n - 1.0);
+                } else {
+                    v = c->use_levc ? c->varCD[o] : c->varD[o];
+                }
                 const double d = v / n;
                 c->discr[o] = d;
                 c->ediv[o] = d * d / (n - 1.0);
@@ -579,12 +588,14 @@ static void film_filter_range(void *vctx, int64_t b, int64_t e) {
 
 void orc_denoise_film_f64(int W, int H, int K, const int32_t *n, const double *stats,
                           const double *varD, const double *varCD, const double *jb, int use_levc,
+                          int discr_source, const double *m2C,
                           int mt_mode, int R, double ds_factor, int lut_n, const double *tcrit2,
                           int nG, const orc_gbuf *gbufs, const double *gmean, const double *film,
                           double *discr, double *filmD, uint32_t *accept_bits, int nthreads) {
     const size_t HW = (size_t)W * H;
     film_ctx c;
     c.W = W; c.H = H; c.K = K; c.R = R; c.nG = nG; c.use_levc = use_levc; c.mt_mode = mt_mode;
+    c.discr_source = discr_source; c.m2C = m2C;
     c.lut_n = lut_n; c.n = n; c.stats = stats; c.varD = varD; c.varCD = varCD; c.jb = jb;
     c.tcrit2 = tcrit2; c.gmean = gmean; c.film = film; c.ds_factor = ds_factor; c.gbufs = gbufs;
     c.discr = discr; c.filmD = filmD; c.accept_bits = accept_bits;
@@ -637,6 +648,12 @@ double orc_tree_sum(const double *v, int64_t len) {
 
 void orc_calc_target_spp(int W, int H, int spp, const int32_t *n, const double *varD,
                          const double *mean, double eps, int tmin, int tmax, int32_t *target) {
+    orc_calc_target_spp_src(W, H, spp, n, varD, NULL, 0, mean, eps, tmin, tmax, target);
+}
+
+void orc_calc_target_spp_src(int W, int H, int spp, const int32_t *n, const double *varD,
+                             const double *m2, int as_source, const double *mean, double eps, int tmin,
+                             int tmax, int32_t *target) {
     const size_t HW = (size_t)W * H;
     double *e = (double *)calloc(HW ? HW : 1, sizeof(double));
     for (size_t p = 0; p < HW; p++) {
@@ -647,7 +664,9 @@ void orc_calc_target_spp(int W, int H, int spp, const int32_t *n, const double *
         const double nn = (double)n[p];
         double acc = 0.0;
         for (int ch = 0; ch < 3; ch++) {
-            double v = varD[(size_t)ch * HW + p] / nn;
+            /* the reference's AS_MODE: denoised variance ("ASM") or the sample variance ("ASN") */
+            const double var = as_source == 1 ? m2[(size_t)ch * HW + p] / (nn - 1.0) : varD[(size_t)ch * HW + p];
+            double v = var / nn;
             if (mean) {
                 const double m = mean[(size_t)ch * HW + p];
                 v = v / (m * m + eps);

@@ -79,19 +79,27 @@ void orc_denoise_vars_f64(int W, int H, int K, int max_moment, const int32_t *n,
                           double *m2C, double *varD, double *varCD, int nthreads);
 
 /* Stage 2c: denoiseFilm. film [3][HW]; outputs discr [K][3][HW], filmD [3][HW].
+ * discr_source 0: the discriminator uses varCD (use_levc) or varD; 1 (the
+ * reference's CASCADE_MODE=0): m2C (use_levc, [K][3][HW]) or the m2 moments,
+ * divided by n - 1.
  * accept_bits (nullable): uint32 [HW][K][words], words = ceil((2R+1)^2/32), bit
  * (dy+R)*(2R+1)+(dx+R) set when the pair test of transform k accepts neighbour
  * (dx,dy) (in-image, valid neighbours only). */
 void orc_denoise_film_f64(int W, int H, int K, const int32_t *n, const double *stats,
                           const double *varD, const double *varCD, const double *jb,
-                          int use_levc, int mt_mode, int R, double ds_factor,
+                          int use_levc, int discr_source, const double *m2C, int mt_mode, int R,
+                          double ds_factor,
                           int lut_n, const double *tcrit2, int nG, const orc_gbuf *gbufs,
                           const double *gmean, const double *film, double *discr,
                           double *filmD, uint32_t *accept_bits, int nthreads);
 
-/* calcTargetSPP: next-round extra samples per pixel. */
+/* calcTargetSPP: next-round extra samples per pixel. as_source 0 ("ASM"): from
+ * varD; 1 ("ASN", the reference's AS_MODE=0): from the sample variance m2/(n-1). */
 void orc_calc_target_spp(int W, int H, int spp, const int32_t *n, const double *varD,
                          const double *mean, double eps, int tmin, int tmax, int32_t *target);
+void orc_calc_target_spp_src(int W, int H, int spp, const int32_t *n, const double *varD,
+                             const double *m2, int as_source, const double *mean, double eps, int tmin,
+                             int tmax, int32_t *target);
 /* Deterministic reduction used by calcTargetSPP: the values are summed in
  * blocks of 1024 (each block: 256 partial sums of 4 strided values, then a
  * pairwise halving tree), and the block sums again the same way until one value

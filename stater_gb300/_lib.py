@@ -22,6 +22,8 @@ TK_IDENTITY, TK_LOG1P, TK_SQRT, TK_CBRT, TK_ASINH, TK_BOXCOX = range(6)
 Q_MEAN, Q_M2, Q_M3, Q_M4, Q_C2X, Q_C2Y, Q_M1 = range(7)
 NQ = 7
 MT_ALL, MT_JB = 2, 3
+DISCR_DENOISED, DISCR_SAMPLE = 0, 1  # the reference's CASCADE_MODE 1 / 0
+AS_DENOISED, AS_SAMPLE = 0, 1        # the reference's AS_MODE 1 ("ASM") / 0 ("ASN")
 ACC_EXACT, ACC_FAST = 0, 1
 
 STATUS = {0: "STATER_OK", 1: "STATER_ERR_INVALID", 2: "STATER_ERR_CUDA", 3: "STATER_ERR_NOMEM",
@@ -73,7 +75,17 @@ class DenoiseFilmArgs(C.Structure):
                 ("mt_mode", C.c_int32), ("use_levc", C.c_int32), ("precision", C.c_int32),
                 ("n", VP), ("film", VP), ("mean", P8), ("varD", P8), ("varCD", P8), ("jb", P8),
                 ("gbuffers", GBuffers), ("discr", P8), ("filmD", VP), ("accept_bits", VP),
-                ("test_order", C.c_int32 * MAX_TRANSFORMS)]
+                ("test_order", C.c_int32 * MAX_TRANSFORMS), ("discr_source", C.c_int32), ("m2", P8), ("m2C", P8)]
+
+
+class TargetSppArgs(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("precision", C.c_int32),
+                ("n", VP), ("m2", VP), ("varD", VP), ("mean", VP), ("eps", C.c_double), ("tmin", C.c_int32),
+                ("tmax", C.c_int32), ("as_source", C.c_int32), ("targetspp", VP)]
+
+
+class PitchedLayout(C.Structure):
+    _fields_ = [("rgb_step", C.c_int64), ("scalar_step", C.c_int64), ("n_step", C.c_int64)]
 
 
 class StaterError(RuntimeError):
@@ -116,11 +128,14 @@ def load() -> C.CDLL:
         "stater_merge_moments": (st, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, VP, VP, VP, VP, VP]),
         "stater_denoise_vars": (st, [C.POINTER(DenoiseVarsArgs), VP]),
         "stater_denoise_film": (st, [C.POINTER(DenoiseFilmArgs), VP]),
+        "stater_denoise_vars_pitched": (st, [C.POINTER(DenoiseVarsArgs), C.POINTER(PitchedLayout), VP]),
+        "stater_denoise_film_pitched": (st, [C.POINTER(DenoiseFilmArgs), C.POINTER(PitchedLayout), VP]),
         "stater_tcrit_lut_intervals": (C.c_int32, []),
         "stater_tcrit2_table": (st, [C.c_double, VP]),
         "stater_t_quantile": (C.c_double, [C.c_double, C.c_double]),
         "stater_calc_target_spp": (st, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, VP, VP, VP, C.c_double,
                                         C.c_int32, C.c_int32, VP, VP]),
+        "stater_calc_target_spp_ex": (st, [C.POINTER(TargetSppArgs), VP]),
         "stater_calc_target_spp_noalloc": (st, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, VP, VP, VP,
                                                 C.c_double, C.c_int32, C.c_int32, VP, VP]),
         "stater_calc_mean_var": (st, [C.c_int32, C.c_int32, VP, VP, VP, VP]),

@@ -175,7 +175,11 @@ class StatBuffers:
     def denoise_film(self, radius: int = 10, filter_sd: float = 10.0, alpha: float = 0.01,
                      gbuffers: Sequence[GBufferSpec] = GBUFFERS_ALBEDO_NORMAL, mt_mode: int = L.MT_ALL,
                      use_levc: bool = False, film: Optional[torch.Tensor] = None,
-                     accept_bits: Optional[torch.Tensor] = None, stream=None) -> None:
+                     accept_bits: Optional[torch.Tensor] = None, cascade: bool = True, stream=None) -> None:
+        """denoiseFilm. cascade=False is the reference's CASCADE_MODE=0 build (the
+        "M" variant): the Welch discriminator uses each pixel's own sample
+        variance (m2, or the LEV-corrected m2C with use_levc) instead of the
+        denoised variance of denoise_vars."""
         a = L.DenoiseFilmArgs()
         a.n_buffers, a.width, a.height = self.K, self.W, self.H
         a.filter_radius, a.ds_factor, a.alpha = int(radius), -0.5 / (filter_sd * filter_sd), float(alpha)
@@ -188,6 +192,9 @@ class StatBuffers:
             a.varCD[k] = _ptr(self.varCD[k])
             a.jb[k] = _ptr(self.jb[k])
             a.discr[k] = _ptr(self.discr[k])
+            a.m2[k] = _ptr(self.stats[k, L.Q_M2])
+            a.m2C[k] = _ptr(self.m2C[k])
+        a.discr_source = L.DISCR_DENOISED if cascade else L.DISCR_SAMPLE
         a.filmD = _ptr(self.filmD)
         a.accept_bits = _ptr(accept_bits)
         a.gbuffers = self._gbuffers(gbuffers)
@@ -198,11 +205,20 @@ class StatBuffers:
         L.call("stater_denoise_film", C.byref(a), _stream_ptr(stream))
 
     def calc_target_spp(self, spp: int, out: torch.Tensor, relative: bool = True, eps: float = 1e-4,
-                        tmin: int = 16, tmax: int = 1024, stream=None) -> None:
+                        tmin: int = 16, tmax: int = 1024, as_source: int = L.AS_DENOISED, stream=None) -> None:
+        """calcTargetSPP. as_source=AS_SAMPLE is the reference's AS_MODE=0 build
+        ("ASN": the sample variance m2 / (n - 1) instead of the denoised varD)."""
         mean = self.stats[0, L.Q_MEAN] if relative else None
-        L.call("stater_calc_target_spp", self.W, self.H, int(spp), self.precision, _ptr(self.n),
-               _ptr(self.varD[0]), _ptr(mean), float(eps), int(tmin), int(tmax), _ptr(out),
-               _stream_ptr(stream))
+        if as_source == L.AS_DENOISED:
+            L.call("stater_calc_target_spp", self.W, self.H, int(spp), self.precision, _ptr(self.n),
+                   _ptr(self.varD[0]), _ptr(mean), float(eps), int(tmin), int(tmax), _ptr(out),
+                   _stream_ptr(stream))
+            return
+        a = L.TargetSppArgs()
+        a.width, a.height, a.spp, a.precision = self.W, self.H, int(spp), self.precision
+        a.n, a.m2, a.varD, a.mean = _ptr(self.n), _ptr(self.stats[0, L.Q_M2]), _ptr(self.varD[0]), _ptr(mean)
+        a.eps, a.tmin, a.tmax, a.as_source, a.targetspp = float(eps), int(tmin), int(tmax), int(as_source), _ptr(out)
+        L.call("stater_calc_target_spp_ex", C.byref(a), _stream_ptr(stream))
 
 
 def bits_words(radius: int) -> int:

@@ -23,7 +23,7 @@ INCLUDE = ROOT / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 EXACT_UNITS = ["accumulate.cu", "denoise.cu", "target_spp.cu", "lev.cu", "film.cu"]
 FAST_UNITS = ["accumulate_fast.cu", "accumulate_tma.cu", "denoise_fast.cu", "lev_fast.cu", "runtime.cu",
-              "server.cu", "probe.cu"]
+              "server.cu", "probe.cu", "pitched.cu"]
 HOST_UNITS = ["tquantile.cpp"]
 
 

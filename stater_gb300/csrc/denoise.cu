@@ -147,7 +147,9 @@ __global__ void film_discr_f64(FilmParams<double> P) {
             e[o] = 0.0;
             continue;
         }
-        const double v = P.use_levc ? P.varCD[k][o] : P.varD[k][o];
+        // CASCADE_MODE: the denoised variance, or the pixel's own sample variance
+        const double v = P.discr_source == STATER_DISCR_SAMPLE ? P.m2s[k][o] / (n - 1.0)
+                                                               : (P.use_levc ? P.varCD[k][o] : P.varD[k][o]);
         const double d = v / n;
         P.discr[k][o] = d;
         e[o] = d * d / (n - 1.0);
@@ -265,8 +267,12 @@ stater_status check_film_args(const stater_denoise_film_args *a) {
     if (a->mt_mode != STATER_MT_ALL && a->mt_mode != STATER_MT_JB)
         return set_error(STATER_ERR_INVALID, "stater_denoise_film: mt_mode must be 2 or 3");
     if (!a->n || !a->film || !a->filmD) return set_error(STATER_ERR_INVALID, "stater_denoise_film: null buffer");
+    if (a->discr_source != STATER_DISCR_DENOISED && a->discr_source != STATER_DISCR_SAMPLE)
+        return set_error(STATER_ERR_INVALID, "stater_denoise_film: discr_source must be 0 or 1");
+    const bool sample = a->discr_source == STATER_DISCR_SAMPLE;
     for (int k = 0; k < a->n_buffers; k++) {
-        if ((k > 0 && !a->mean[k]) || !a->discr[k] || (a->use_levc ? !a->varCD[k] : !a->varD[k]))
+        const void *var = sample ? (a->use_levc ? a->m2C[k] : a->m2[k]) : (a->use_levc ? a->varCD[k] : a->varD[k]);
+        if ((k > 0 && !a->mean[k]) || !a->discr[k] || !var)
             return set_error(STATER_ERR_INVALID, "stater_denoise_film: null buffer pointer");
         if (a->mt_mode == STATER_MT_JB && !a->jb[k])
             return set_error(STATER_ERR_INVALID, "stater_denoise_film: mt_mode 3 needs jb");
@@ -337,6 +343,7 @@ stater_status stater_denoise_film(const stater_denoise_film_args *a, stater_stre
     P.R = a->filter_radius;
     P.mt_mode = a->mt_mode;
     P.use_levc = a->use_levc;
+    P.discr_source = a->discr_source;
     P.lut_n = tcrit_intervals();
     P.ds = (double)a->ds_factor;
     P.n = a->n;
@@ -347,6 +354,7 @@ stater_status stater_denoise_film(const stater_denoise_film_args *a, stater_stre
         P.varCD[k] = (const double *)a->varCD[k];
         P.jb[k] = (const double *)a->jb[k];
         P.discr[k] = (double *)a->discr[k];
+        P.m2s[k] = (const double *)(a->use_levc ? a->m2C[k] : a->m2[k]);
     }
     P.filmD = (double *)a->filmD;
     P.bits = a->accept_bits;

@@ -74,12 +74,12 @@ struct FastVars {
 };
 
 struct FastFilm {
-    int W, H, K, R, mt_mode, use_levc, lut_n;
+    int W, H, K, R, mt_mode, use_levc, lut_n, discr_source;
     float ds2;
     const int32_t *n;
     const float *film;
     const float *mean[STATER_MAX_TRANSFORMS];
-    const float *var[STATER_MAX_TRANSFORMS];  // varCD or varD
+    const float *var[STATER_MAX_TRANSFORMS];  // varCD or varD; m2C or m2 with STATER_DISCR_SAMPLE
     const float *jb[STATER_MAX_TRANSFORMS];
     const float *lut;    // [lut_n + 1] t2 over u
     const float *tlo;    // [kDfMax + 1] lower envelope of t2 at integer df
@@ -335,7 +335,9 @@ __global__ void film_discr_f32(FastFilm P) {
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         const size_t o = (size_t)c * HW + p;
-        P.discr[k][o] = nn < 2 ? 0.f : P.var[k][o] / (float)nn;
+        // CASCADE_MODE: the denoised variance, or the pixel's own sample variance
+        const float v = P.discr_source == STATER_DISCR_SAMPLE ? P.var[k][o] / ((float)nn - 1.f) : P.var[k][o];
+        P.discr[k][o] = nn < 2 ? 0.f : v / (float)nn;
     }
 }
 
@@ -1273,13 +1275,15 @@ stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s
     P.R = a->filter_radius;
     P.mt_mode = a->mt_mode;
     P.use_levc = a->use_levc;
+    P.discr_source = a->discr_source;
     P.lut_n = tcrit_intervals();
     P.ds2 = a->ds_factor * kLog2e;
     P.n = a->n;
     P.film = (const float *)a->film;
     for (int k = 0; k < STATER_MAX_TRANSFORMS; k++) {
         P.mean[k] = (const float *)a->mean[k];
-        P.var[k] = (const float *)(a->use_levc ? a->varCD[k] : a->varD[k]);
+        P.var[k] = (const float *)(a->discr_source == STATER_DISCR_SAMPLE ? (a->use_levc ? a->m2C[k] : a->m2[k])
+                                                                          : (a->use_levc ? a->varCD[k] : a->varD[k]));
         P.jb[k] = (const float *)a->jb[k];
         P.discr[k] = (float *)a->discr[k];
     }

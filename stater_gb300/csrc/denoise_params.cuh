@@ -39,13 +39,14 @@ struct VarsParams {
 
 template <typename T>
 struct FilmParams {
-    int W, H, K, R, mt_mode, use_levc, lut_n;
+    int W, H, K, R, mt_mode, use_levc, lut_n, discr_source;
     T ds;
     const int32_t *n;
     const T *film;
     const T *mean[STATER_MAX_TRANSFORMS];
     const T *varD[STATER_MAX_TRANSFORMS];
     const T *varCD[STATER_MAX_TRANSFORMS];
+    const T *m2s[STATER_MAX_TRANSFORMS];  // STATER_DISCR_SAMPLE: m2C (use_levc) or m2
     const T *jb[STATER_MAX_TRANSFORMS];
     const T *lut;
     GBuf<T> gb;

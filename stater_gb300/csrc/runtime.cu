@@ -250,8 +250,16 @@ void stater_print_macro_configuration(void) {
     std::printf("MAX_GBUFFERS = %d\n", STATER_MAX_GBUFFERS);
     std::printf("MAX_RADIUS = %d\n", STATER_MAX_RADIUS);
     std::printf("TCRIT_LUT_INTERVALS = %d\n", kLutIntervals);
-    std::printf("FILM_MULTI_TRANSFORM_MODE = per call (2 = all, 3 = Jarque-Bera select)\n");
-    std::printf("USE_LEVC = per call (use_levc)\n");
+    std::printf("FULL_MULTI_TRANSFORM = per call (n_transforms 1..%d, Box-Cox lambdas or named transforms)\n",
+                STATER_MAX_TRANSFORMS);
+    std::printf("FILM_MULTI_TRANSFORM_MODE = per call (mt_mode: 2 = all transforms, 3 = Jarque-Bera select)\n");
+    std::printf("USE_LEVC = per call (use_levc: 1 = LEV-corrected varCD / m2C)\n");
+    std::printf("CASCADE_MODE = per call (discr_source: 0 = denoised variance [CASCADE_MODE=1], "
+                "1 = sample variance [CASCADE_MODE=0])\n");
+    std::printf("AS_MODE = per call (stater_calc_target_spp_ex as_source: 0 = ASM denoised varD, "
+                "1 = ASN sample variance)\n");
+    std::printf("variants: MCL = cascade + LEV (default); MC = cascade; M = neither; ASN+MCL = as_source 1; "
+                "MT-JB = mt_mode 3\n");
     std::printf("PRECISION = per call (F64 plain form, F32 form)\n");
     std::printf("==== end ====\n");
 }

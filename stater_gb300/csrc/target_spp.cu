@@ -36,6 +36,31 @@ __global__ void tspp_error_kernel(size_t HW, const int32_t *__restrict__ n, cons
     e[p] = acc;
 }
 
+// AS_MODE=0 ("ASN"): the error estimate from the pixel's sample variance m2 / (n - 1).
+template <typename T>
+__global__ void tspp_error_sample_kernel(size_t HW, const int32_t *__restrict__ n, const T *__restrict__ m2,
+                                         const T *__restrict__ mean, double eps, double *e) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= HW) return;
+    const int nn = n[p];
+    if (nn < 2) {
+        e[p] = 0.0;
+        return;
+    }
+    const double nd = (double)nn;
+    double acc = 0.0;
+    for (int c = 0; c < 3; c++) {
+        const double var = (double)m2[(size_t)c * HW + p] / (nd - 1.0);
+        double v = var / nd;
+        if (mean) {
+            const double m = (double)mean[(size_t)c * HW + p];
+            v = v / (m * m + eps);
+        }
+        acc = acc + v;
+    }
+    e[p] = acc;
+}
+
 __global__ void tree_block_kernel(const double *__restrict__ in, long long len, double *out) {
     __shared__ double part[256];
     const int t = threadIdx.x;
@@ -116,6 +141,54 @@ extern "C" stater_status stater_calc_target_spp(int32_t width, int32_t height, i
         len = nb;
     }
     tspp_target_kernel<<<grid, 256, 0, s>>>(HW, spp, n, e, cur, tmin, tmax, targetspp);
+    STATER_CHECK_LAUNCH("tspp_target_kernel");
+    return STATER_OK;
+}
+
+extern "C" stater_status stater_calc_target_spp_ex(const stater_target_spp_args *a, stater_stream stream) {
+    clear_error();
+    if (!a) return set_error(STATER_ERR_INVALID, "stater_calc_target_spp_ex: null args");
+    if (a->as_source == STATER_AS_DENOISED)
+        return stater_calc_target_spp(a->width, a->height, a->spp, a->precision, a->n, a->varD, a->mean, a->eps,
+                                      a->tmin, a->tmax, a->targetspp, stream);
+    if (a->as_source != STATER_AS_SAMPLE)
+        return set_error(STATER_ERR_INVALID, "stater_calc_target_spp_ex: as_source must be 0 or 1");
+    if (a->width <= 0 || a->height <= 0 || a->spp < 0 || !a->n || !a->m2 || !a->targetspp || a->tmin < 0 ||
+        a->tmax < a->tmin || !(a->eps >= 0.0))
+        return set_error(STATER_ERR_INVALID, "stater_calc_target_spp_ex: bad arguments");
+    if (a->precision != STATER_F64 && a->precision != STATER_F32)
+        return set_error(STATER_ERR_INVALID, "stater_calc_target_spp_ex: bad precision");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t HW = (size_t)a->width * a->height;
+    const size_t nb1 = (HW + 1023) / 1024;
+    double *e = (double *)scratch(2, sizeof(double) * (HW + 2 * nb1 + 2), s);
+    if (!e) return set_error(STATER_ERR_NOMEM, "stater_calc_target_spp_ex: scratch allocation failed");
+    double *bufA = e + HW, *bufB = bufA + nb1 + 1;
+    const unsigned grid = (unsigned)((HW + 255) / 256);
+    if (a->precision == STATER_F64)
+        tspp_error_sample_kernel<double><<<grid, 256, 0, s>>>(HW, a->n, (const double *)a->m2,
+                                                              (const double *)a->mean, a->eps, e);
+    else
+        tspp_error_sample_kernel<float><<<grid, 256, 0, s>>>(HW, a->n, (const float *)a->m2, (const float *)a->mean,
+                                                             a->eps, e);
+    STATER_CHECK_LAUNCH("tspp_error_sample_kernel");
+    const double *cur = e;
+    long long len = (long long)HW;
+    double *dst = bufA;
+    if (len == 1) {
+        cudaError_t ce = cudaMemcpyAsync(bufA, e, sizeof(double), cudaMemcpyDeviceToDevice, s);
+        if (ce != cudaSuccess) return cuda_status(ce, "stater_calc_target_spp_ex copy");
+        cur = bufA;
+    }
+    while (len > 1) {
+        const long long nb = (len + 1023) / 1024;
+        tree_block_kernel<<<(unsigned)nb, 256, 0, s>>>(cur, len, dst);
+        STATER_CHECK_LAUNCH("tree_block_kernel");
+        cur = dst;
+        dst = (dst == bufA) ? bufB : bufA;
+        len = nb;
+    }
+    tspp_target_kernel<<<grid, 256, 0, s>>>(HW, a->spp, a->n, e, cur, a->tmin, a->tmax, a->targetspp);
     STATER_CHECK_LAUNCH("tspp_target_kernel");
     return STATER_OK;
 }

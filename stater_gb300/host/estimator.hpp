@@ -152,8 +152,13 @@ struct EstimatorConfig {
     float mean_z_value = 1.95996f;   // "meanzvalue": accepted and, as in the reference, without effect
     float var_z_value = 2.80703f;    // "varzvalue" (statpath.cpp:1070)
     double alpha = 0.01;             // two-sided level of the Welch test
-    int mt_mode = STATER_MT_ALL;
-    bool use_levc = false;
+    // The reference's build variants (scripts/alternate-builds/*.sh), as runtime
+    // switches: MCL = cascade + use_levc (the reference's default build), MC =
+    // cascade only, M = neither; ASM / ASN = as_source; MT-JB = mt_mode 3.
+    int mt_mode = STATER_MT_ALL;     // FILM_MULTI_TRANSFORM_MODE
+    bool use_levc = true;            // USE_LEVC (needs max_moment 5: c2X, c2Y)
+    bool cascade = true;             // CASCADE_MODE
+    int as_source = STATER_AS_DENOISED;  // AS_MODE: ASM (denoised varD) or ASN (sample variance)
     bool enable_as = false;          // "enableas": CalcTargetSPPs output downloaded
     bool denoise_film = true;        // "denoisefilm": film uploaded / filmD downloaded
     stater_precision precision = STATER_F32;
@@ -323,6 +328,7 @@ class Estimator {
         a.alpha = (float)cfg.alpha;
         a.mt_mode = cfg.mt_mode;
         a.use_levc = cfg.use_levc ? 1 : 0;
+        a.discr_source = cfg.cascade ? STATER_DISCR_DENOISED : STATER_DISCR_SAMPLE;
         a.precision = cfg.precision;
         a.n = n_ptr();
         a.film = film_for_precision();
@@ -332,6 +338,8 @@ class Estimator {
             a.varCD[k] = out(12, k);
             a.jb[k] = out(7, k);
             a.discr[k] = out(13, k);
+            a.m2[k] = stat(k, STATER_Q_M2);
+            a.m2C[k] = out(10, k);
         }
         a.gbuffers = gbuffers(meanG);
         a.filmD = filmD_.get();
@@ -350,10 +358,22 @@ class Estimator {
 
     // stat_denoiser::calcTargetSPP (estimator.cpp:498-513).
     void CalcTargetSPPs(uint64_t spp) {
-        check(stater_calc_target_spp(width, height, (int32_t)spp, cfg.precision, n_ptr(), out(11, 0),
-                                     stat(0, STATER_Q_MEAN), cfg.target_eps, cfg.target_min, cfg.target_max,
-                                     (int32_t *)targetSPPBuffer.device, (stater_stream)stream),
-              "Estimator::CalcTargetSPPs");
+        stater_target_spp_args a;
+        std::memset(&a, 0, sizeof(a));
+        a.width = width;
+        a.height = height;
+        a.spp = (int32_t)spp;
+        a.precision = cfg.precision;
+        a.n = n_ptr();
+        a.m2 = stat(0, STATER_Q_M2);
+        a.varD = out(11, 0);
+        a.mean = stat(0, STATER_Q_MEAN);
+        a.eps = cfg.target_eps;
+        a.tmin = cfg.target_min;
+        a.tmax = cfg.target_max;
+        a.as_source = cfg.as_source;
+        a.targetspp = (int32_t *)targetSPPBuffer.device;
+        check(stater_calc_target_spp_ex(&a, (stater_stream)stream), "Estimator::CalcTargetSPPs");
     }
 
     void Synchronize() { check(stater_synchronize((stater_stream)stream), "Estimator::Synchronize"); }

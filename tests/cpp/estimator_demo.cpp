@@ -31,6 +31,8 @@ static EstimatorConfig config(int radius) {
     c.filter_radius = radius;
     c.enable_as = true;
     c.denoise_film = true;
+    c.use_levc = false;  // the MC variant, as the Python side of the test runs it
+    c.cascade = true;
     c.precision = STATER_F32;
     c.acc_mode = STATER_ACC_FAST;
     return c;

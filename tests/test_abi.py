@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(lib):
 def test_host_only_entry_points(lib):
     import ctypes
     import numpy as np
-    assert lib.stater_abi_version() == 1
+    assert lib.stater_abi_version() == 2
     n = lib.stater_tcrit_lut_intervals()
     t = np.zeros(n + 1)
     assert lib.stater_tcrit2_table(ctypes.c_double(0.01), t.ctypes.data_as(ctypes.c_void_p)) == 0

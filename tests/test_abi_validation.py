@@ -111,3 +111,43 @@ def test_pipeline_wait_hook_rejects(lib):
     assert lib.stater_debug_set_pipeline_waits(100, 2) == INVALID
     assert lib.stater_debug_set_pipeline_waits(256, 0) == 0
     assert lib.stater_debug_set_pipeline_waits(0, 0) == 0
+
+
+def test_pitched_entry_points_reject_bad_layouts(lib):
+    va = L.DenoiseVarsArgs()
+    va.n_buffers, va.width, va.height, va.max_moment, va.precision = 1, 64, 8, 3, L.F32
+    lay = L.PitchedLayout()
+    lay.rgb_step, lay.scalar_step, lay.n_step = 3 * 64 * 4 - 4, 64 * 4, 64 * 4
+    assert lib.stater_denoise_vars_pitched(C.byref(va), C.byref(lay), None) == INVALID
+    assert b"rgb_step" in lib.stater_last_error()
+    lay.rgb_step, lay.n_step = 3 * 64 * 4, 64 * 4 - 4
+    assert lib.stater_denoise_vars_pitched(C.byref(va), C.byref(lay), None) == INVALID
+    assert b"n_step" in lib.stater_last_error()
+    fa = L.DenoiseFilmArgs()
+    fa.n_buffers, fa.width, fa.height, fa.precision = 1, 64, 8, L.F64
+    lay.rgb_step, lay.scalar_step, lay.n_step = 3 * 64 * 4, 64 * 8, 64 * 4  # rgb_step too short for doubles
+    assert lib.stater_denoise_film_pitched(C.byref(fa), C.byref(lay), None) == INVALID
+    assert lib.stater_denoise_film_pitched(C.byref(fa), None, None) == INVALID
+
+
+def test_target_spp_ex_rejects(lib):
+    a = L.TargetSppArgs()
+    a.width, a.height, a.spp, a.precision, a.tmin, a.tmax = 8, 8, 16, L.F32, 16, 1024
+    a.n, a.targetspp = 16, 16  # never dereferenced
+    a.as_source = 2
+    assert lib.stater_calc_target_spp_ex(C.byref(a), None) == INVALID
+    a.as_source = L.AS_SAMPLE  # needs m2
+    assert lib.stater_calc_target_spp_ex(C.byref(a), None) == INVALID
+    assert b"bad arguments" in lib.stater_last_error()
+
+
+def test_denoise_film_rejects_bad_discr_source(lib):
+    fa = L.DenoiseFilmArgs()
+    fa.n_buffers, fa.width, fa.height, fa.filter_radius, fa.alpha, fa.mt_mode = 1, 8, 8, 2, 0.01, 2
+    fa.n, fa.film, fa.filmD = 16, 16, 16
+    fa.discr[0], fa.varD[0] = 16, 16
+    fa.discr_source = 3
+    assert lib.stater_denoise_film(C.byref(fa), None) == INVALID
+    assert b"discr_source" in lib.stater_last_error()
+    fa.discr_source = L.DISCR_SAMPLE  # needs m2
+    assert lib.stater_denoise_film(C.byref(fa), None) == INVALID

@@ -79,8 +79,10 @@ def test_lev_matches_numpy_lstsq():
                 assert np.allclose(out["beta"][c, :, y, x], beta, rtol=1e-7, atol=1e-9)
 
 
-def _py_denoise(n, stats, gmean, mm, R, ds, z, gspec, alpha, mt_mode, use_levc, lut):
-    """Pure-Python restatement of both filters (small images only)."""
+def _py_denoise(n, stats, gmean, mm, R, ds, z, gspec, alpha, mt_mode, use_levc, lut, discr_source=0):
+    """Pure-Python restatement of both filters (small images only). discr_source
+    1: the Welch discriminator from the pixel's own sample variance (the
+    reference's CASCADE_MODE=0) instead of the denoised one."""
     K, _, _, H, W = stats.shape
     s2 = np.zeros((K, 3, H, W)); s2c = np.zeros_like(s2); ln = np.zeros_like(s2); se = np.zeros_like(s2)
     jb = np.zeros((K, H, W))
@@ -125,7 +127,10 @@ def _py_denoise(n, stats, gmean, mm, R, ds, z, gspec, alpha, mt_mode, use_levc, 
                             ww = w(y, x, yy, xx)
                             sw += ww; sv += ww * s2[k, c, yy, xx]; svc += ww * s2c[k, c, yy, xx]
                     varD[k, c, y, x] = sv / sw; varCD[k, c, y, x] = svc / sw
-    v = varCD if use_levc else varD
+    if discr_source == 1:
+        v = s2c if use_levc else s2
+    else:
+        v = varCD if use_levc else varD
     d = v / n[None, None]
     e = d * d / (n[None, None] - 1)
     film = stats[0, 0]
@@ -162,8 +167,9 @@ def _py_denoise(n, stats, gmean, mm, R, ds, z, gspec, alpha, mt_mode, use_levc, 
     return dict(jb=jb, lnS2=ln, se2=se, varD=varD, varCD=varCD, filmD=filmD, discr=d)
 
 
-@pytest.mark.parametrize("mm,mt_mode,use_levc", [(3, 2, False), (5, 2, True), (5, 3, False)])
-def test_filters_match_python_restatement(mm, mt_mode, use_levc):
+@pytest.mark.parametrize("mm,mt_mode,use_levc,discr_source", [(3, 2, False, 0), (5, 2, True, 0), (5, 3, False, 0),
+                                                               (3, 2, False, 1), (5, 2, True, 1)])
+def test_filters_match_python_restatement(mm, mt_mode, use_levc, discr_source):
     W, H, G, S, R = 7, 6, 7, 24, 2
     smp = synth_samples(W, H, S, G=G, seed=21, region=3, noise_sigma=0.3)
     tr = ["identity", "log1p", "sqrt"]
@@ -175,9 +181,9 @@ def test_filters_match_python_restatement(mm, mt_mode, use_levc):
     v = oracle.denoise_vars(n, st, gm, mm, R, ds, z, gspec)
     lut = oracle.tcrit2_table(0.01)
     f = oracle.denoise_film(n, st, v["varD"], v["varCD"], v["jb"], gm, st[0, 0], R, ds, 0.01, gspec,
-                            mt_mode=mt_mode, use_levc=use_levc, lut=lut)
+                            mt_mode=mt_mode, use_levc=use_levc, lut=lut, discr_source=discr_source, m2C=v["m2C"])
     gpy = [(a, b, float(np.float32(-0.5 / (s * s)))) for a, b, s in gspec]
-    py = _py_denoise(n, st, gm, mm, R, ds, z, gpy, 0.01, mt_mode, use_levc, lut)
+    py = _py_denoise(n, st, gm, mm, R, ds, z, gpy, 0.01, mt_mode, use_levc, lut, discr_source)
     for key in ("jb", "lnS2", "se2", "varD", "varCD"):
         assert np.allclose(v[key], py[key], rtol=1e-12, atol=1e-300), key
     assert np.allclose(f["discr"], py["discr"], rtol=1e-12)
@@ -196,6 +202,18 @@ def test_target_spp_budget_and_clamp():
     assert t2.min() >= 16 and t2.max() <= 1024
     n[0, 0] = 1
     assert oracle.calc_target_spp(n, varD, mean, spp=64)[0, 0] == 1024
+
+
+def test_target_spp_sample_variance_source():
+    """ASN (the reference's AS_MODE=0) ranks pixels by the sample variance m2/(n-1)."""
+    rng = np.random.default_rng(10)
+    H, W = 23, 29
+    n = rng.integers(16, 64, size=(H, W)).astype(np.int32)
+    m2 = rng.random((3, H, W)) * 5
+    mean = rng.random((3, H, W)) + 0.1
+    asn = oracle.calc_target_spp(n, None, mean, spp=64, m2=m2, as_source=1)
+    asm = oracle.calc_target_spp(n, m2 / (n[None] - 1.0), mean, spp=64)
+    assert np.array_equal(asn, asm)
 
 
 def test_mean_var_f32_matches_formula():
