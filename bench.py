@@ -520,12 +520,32 @@ def run_gpu(args, rank, world, dist):
         torch.cuda.synchronize()
         e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
         e2e_val = world * HW / (max_over_ranks(e2e_ms, world, dist) / 1e3) / 1e6
-        e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": SPP * (5 + G) * HW * 4,
+        h2d = SPP * (5 + G) * HW * 4
+        # the host link alone: the same chunk copies, nothing else on the GPU
+        l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        l0.record(copy_stream)
+        for ci, c0 in enumerate(range(0, SPP, chunk)):
+            with torch.cuda.stream(copy_stream):
+                stage[ci % 2].copy_(host[c0:c0 + chunk], non_blocking=True)
+        l1.record(copy_stream)
+        torch.cuda.synchronize()
+        link_gbs = h2d / (l0.elapsed_time(l1) / 1e3) / 1e9
+        e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 3 * HW * 4, "ms_per_step": e2e_ms,
+               "h2d_gbs": h2d / (e2e_ms / 1e3) / 1e9, "link_gbs_copies_alone": link_gbs,
                "path": "pinned host samples -> 32-spp chunks (copy stream) -> accumulate + film sums -> film image "
                        "-> denoise -> filmD to host"}
         del host, stage
         torch.cuda.empty_cache()
+
+    # the other configurations, compact: LEV at 1080p/512 spp, adaptive rounds,
+    # one serving rate (each with its own clock record)
+    if not args.no_configs:
+        extra["lev"] = measure_lev(S, 1920, 1080, 512, steps=3, warmup=1)
+        extra["adaptive"] = measure_adaptive(S, steps=3, warmup=1, chunk=32)
+        extra["serving"] = measure_serving(S, njobs=args.serve_jobs, rate=200.0, slots=4, chunk=32)
+        extra["batch"] = measure_batch(S)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -598,6 +618,167 @@ def run_serving_trace(S, jobs, rate, slots, precision, with_output=True, seed=1,
     return st
 
 
+def measure_adaptive(S, steps, warmup, chunk, with_plain=False):
+    """Adaptive sampling at 1080p through the serving engine: 16 spp, then 3
+    rounds of 64 extra spp on average (targets from calcTargetSPP, clamped to
+    [16, 1024]), K = 5, R = 10, moment buffers resident between rounds. One job
+    at a time; the job's latency is the step."""
+    import numpy as np
+
+    from stater_gb300 import serving
+    W, H = 1920, 1080
+    job = dict(width=W, height=H, spp=16, rounds=4, round_spp=64, transforms=tuple(WORKLOAD["transforms"]),
+               radius=WORKLOAD["radius"], seed=5)
+    res = {}
+    precs = ((S.F32, "f32"), (S.F64, "f64")) if with_plain else ((S.F32, "f32"),)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        for prec, name in precs:
+            lat = []
+            with serving.Server(max_slots=1, precision=prec, chunk_spp=chunk) as srv:
+                for it in range(warmup + steps if prec == S.F32 else 2):
+                    out = np.zeros((3, H, W), np.float32) if prec == S.F32 else None
+                    jid = srv.submit(serving.job_desc(**job, out=out), keepalive=out)
+                    srv.wait(jid, 3600)
+                    lat.append(srv.poll(jid)[1])
+            res[name] = lat[-steps:] if prec == S.F32 else lat[-1:]
+    ms = statistics.median(res["f32"])
+    r = {"value": W * H / ms / 1e3, "unit": UNIT, "ms": ms,
+         "workload": "1920x1080, 16 spp then 3 rounds of 64 extra spp on average, clamped to [16, 1024] per pixel "
+                     "by relative variance; K=5, R=10; moment buffers resident between rounds",
+         "latency_ms": {"p50": ms, "p99": float(np.percentile(res["f32"], 99))}, "clocks": clk.summary()}
+    if with_plain:
+        r["plain_f64"] = {"ms_per_job": res["f64"][0], "value": W * H / res["f64"][0] / 1e3}
+        r["speedup_vs_plain_f64"] = res["f64"][0] / ms
+    return r
+
+
+def measure_lev(S, W, H, SPP, steps, warmup, with_plain=False):
+    """LEV: per-pixel ridge regression of RGB on 7 features + intercept, all SPP
+    samples resident in HBM and accumulated in one call, then the FP64 solve."""
+    import torch
+    G = 7
+    smp = S.generate_samples(W, H, SPP, n_features=G, seed=9, lev_r2=0.6)
+    res = {}
+    stream = torch.cuda.current_stream()
+    precs = ((S.F32, "f32"), (S.F64, "f64")) if with_plain else ((S.F32, "f32"),)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        for prec, name in precs:
+            lev = S.LevState(W, H, G, prec)
+            times, acc_times = [], []
+            em = torch.cuda.Event(enable_timing=True)
+            for it in range(warmup + steps if prec == S.F32 else 2):
+                lev.state.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                lev.accumulate(smp)
+                em.record(stream)
+                lev.solve(1e-6)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1))
+                acc_times.append(e0.elapsed_time(em))
+            res[name] = statistics.median(times[-steps:]) if prec == S.F32 else times[-1]
+            res[name + "_acc"] = statistics.median(acc_times[-steps:]) if prec == S.F32 else acc_times[-1]
+            res[name + "_r2"] = float(lev.r2.double().median().item())
+            del lev
+    del smp
+    torch.cuda.empty_cache()
+    acc_bytes = W * H * SPP * (G + 3) * 4
+    acc_gbs = acc_bytes / (res["f32_acc"] / 1e3) / 1e9
+    hbm_peak, peak_source = hbm_peak_gbs()
+    # DRAM bytes per launch from one ncu capture of lev_tma_f32 at 480x272, 64 spp:
+    # 406.1 MB read + 58.7 MB written, of which the per-pixel state is 58.7 MB each
+    # way (scaled by pixels) and the rest sample planes (scaled by pixel-samples).
+    state_b, samp_b = 58.726656e6, 406.123520e6 - 58.726656e6
+    traffic = (2 * state_b * (W * H) / (480 * 272) + samp_b * (W * H * SPP) / (480 * 272 * 64)) / 1e9
+    r = {"value": W * H / res["f32"] / 1e3, "unit": UNIT, "ms": res["f32"],
+         "workload": f"{W}x{H}, {SPP} spp, 7 features + intercept, ridge lambda 1e-6, samples resident in HBM "
+                     f"({W * H * SPP * (5 + G) * 4 / 1e9:.1f} GB of planes, {acc_bytes / 1e9:.1f} GB read by the "
+                     "regression)",
+         "stage_ms": {"accumulate": res["f32_acc"], "solve": res["f32"] - res["f32_acc"]},
+         "roofline": {"kernel": "lev_tma_f32", "bound": "hbm", "achieved": acc_gbs, "peak": hbm_peak, "unit": "GB/s",
+                      "frac": acc_gbs / hbm_peak, "traffic": traffic, "algorithmic_gb": acc_bytes / 1e9,
+                      "peak_source": peak_source},
+         "median_r2": res["f32_r2"], "clocks": clk.summary()}
+    if with_plain:
+        r["plain_f64"] = {"ms_per_step": res["f64"], "median_r2": res["f64_r2"]}
+        r["speedup_vs_plain_f64"] = res["f64"] / res["f32"]
+    return r
+
+
+def measure_batch(S, njobs=32, steps=5, seed=11):
+    """Many small images (256x256 and 512x512; 16 or 64 spp; K = 1, 3 or 5;
+    21x21 window), samples resident in HBM: one step denoises all of them from
+    zeroed statistics, either as the per-image call sequence on one stream
+    (accumulate + film sums, film image, denoiseVars, denoiseFilm) or as one
+    batch (one launch per denoise stage for all images, replayed as a CUDA
+    graph). Same bits either way."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(seed)
+    tr = WORKLOAD["transforms"]
+    jobs = []
+    for i in range(njobs):
+        side = int(rng.choice([256, 512]))
+        spp = int(rng.choice([16, 64]))
+        k = int(rng.choice([1, 3, 5]))
+        smp = S.generate_samples(side, side, spp, n_features=7, seed=500 + i)
+        b = S.StatBuffers(side, side, tr[:k], 7, 3, S.F32)
+        film = S.Film(side, side, n_features=7)
+        jobs.append(dict(buffers=b, film=film, samples=smp, radius=WORKLOAD["radius"], gbuffers=_specs(S)))
+    pixels = sum(j["buffers"].HW for j in jobs)
+    stream = torch.cuda.current_stream()
+
+    def sequential():
+        for j in jobs:
+            b, film = j["buffers"], j["film"]
+            _reset(b, film)
+            b.accumulate(j["samples"], mode=S.ACC_FAST, film=film)
+            rgb = film.update_image()
+            b.denoise_vars(radius=j["radius"], gbuffers=j["gbuffers"])
+            b.denoise_film(radius=j["radius"], gbuffers=j["gbuffers"], film=rgb)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        ev[0].record(stream)
+        for i in range(steps):
+            fn()
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+        return [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        seq = timed(sequential)
+        batch = S.Batch(jobs, reset=True)
+        bat = timed(batch.run)
+    batch.close()
+    seq_ms, bat_ms = statistics.median(seq), statistics.median(bat)
+    out = {"value": pixels / bat_ms / 1e3, "unit": UNIT, "ms_per_step": bat_ms, "jobs": njobs,
+           "pixels": pixels, "per_image_calls": {"value": pixels / seq_ms / 1e3, "ms_per_step": seq_ms},
+           "speedup_vs_per_image_calls": seq_ms / bat_ms,
+           "latency_ms": {"p50": float(np.percentile(bat, 50)), "p99": float(np.percentile(bat, 99))},
+           "workload": f"{njobs} images of 256x256 or 512x512, 16 or 64 spp, K 1/3/5, R 10, samples resident",
+           "clocks": clk.summary()}
+    del jobs
+    torch.cuda.empty_cache()
+    return out
+
+
+def measure_serving(S, njobs, rate, slots, chunk, seed=0):
+    """One Poisson arrival rate of the mixed-job trace through the serving engine."""
+    jobs = serving_trace(njobs, seed=seed)
+    run_serving_trace(S, serving_trace(4, seed=99)[:4], 0, slots, S.F32)  # warm-up: scratch, tables
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        st = run_serving_trace(S, jobs, rate, slots, S.F32, chunk=chunk)
+    return {"value": st["mpix_per_s"], "unit": UNIT, "rate_jobs_per_s": rate, "jobs": njobs, "slots": slots,
+            "latency_ms": {"p50": st["latency_p50_ms"], "p99": st["latency_p99_ms"], "mean": st["latency_mean_ms"]},
+            "completed": st["completed"], "failed": st["failed"], "peak_footprint_gb": st["peak_footprint_bytes"] / 1e9,
+            "workload": f"{njobs} jobs, resolutions {SERVE_RES}, spp {SERVE_SPP}, K {SERVE_K}, Poisson arrivals",
+            "clocks": clk.summary()}
+
+
 def run_config(args, rank, world, dist):
     import numpy as np
     import torch
@@ -643,76 +824,23 @@ def run_config(args, rank, world, dist):
                                                             "p99": f64_small["latency_p99_ms"]}},
                 "clocks": clk.summary()}
     elif args.config == "adaptive":
-        from stater_gb300 import serving
-        W, H = 1920, 1080
-        job = dict(width=W, height=H, spp=16, rounds=4, round_spp=64, transforms=tuple(WORKLOAD["transforms"]),
-                   radius=WORKLOAD["radius"], seed=5)
-        res = {}
-        for prec, name in ((S.F32, "f32"), (S.F64, "f64")):
-            lat = []
-            with serving.Server(max_slots=1, precision=prec, chunk_spp=args.chunk) as srv:
-                for it in range(args.warmup + args.steps if prec == S.F32 else 2):
-                    out = np.zeros((3, H, W), np.float32) if prec == S.F32 else None
-                    jid = srv.submit(serving.job_desc(**job, out=out), keepalive=out)
-                    srv.wait(jid, 3600)
-                    lat.append(srv.poll(jid)[1])
-            res[name] = lat[-args.steps:] if prec == S.F32 else lat[-1:]
-        ms = statistics.median(res["f32"])
-        line = {"metric": "Mpix/s denoised, adaptive sampling 1080p 4 rounds", "value": W * H / ms / 1e3, "unit": UNIT,
-                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        r = measure_adaptive(S, args.steps, args.warmup, args.chunk, with_plain=True)
+        line = {"metric": "Mpix/s denoised, adaptive sampling 1080p 4 rounds", "value": r["value"], "unit": UNIT,
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded on-device generation)",
-                "config": {"workload": "1920x1080, 16 spp then 3 rounds of 64 extra spp on average, clamped to [16, 1024] "
-                                       "per pixel by relative variance; K=5, R=10; moment buffers resident between rounds"},
-                "latency_ms": {"p50": ms, "p99": float(np.percentile(res["f32"], 99))},
-                "plain_f64": {"ms_per_job": res["f64"][0], "value": W * H / res["f64"][0] / 1e3},
-                "speedup_vs_plain_f64": res["f64"][0] / ms}
+                "data": "synthetic (seeded on-device generation)", "config": {"workload": r["workload"]},
+                "latency_ms": r["latency_ms"], "plain_f64": r["plain_f64"],
+                "speedup_vs_plain_f64": r["speedup_vs_plain_f64"], "clocks": r["clocks"]}
     elif args.config == "lev":
-        W, H, SPP, G = args.width or 1920, args.height or 1080, args.spp or 512, 7
-        # all 512 samples resident (51 GB of planes at 1080p) and accumulated in one call
-        chunks = [S.generate_samples(W, H, SPP, n_features=G, seed=9, lev_r2=0.6)]
-        res = {}
-        stream = torch.cuda.current_stream()
-        for prec, name in ((S.F32, "f32"), (S.F64, "f64")):
-            lev = S.LevState(W, H, G, prec)
-            times, acc_times = [], []
-            em = torch.cuda.Event(enable_timing=True)
-            for it in range(args.warmup + args.steps if prec == S.F32 else 2):
-                lev.state.zero_()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                for c in chunks:
-                    lev.accumulate(c)
-                em.record(stream)
-                lev.solve(1e-6)
-                e1.record(stream)
-                torch.cuda.synchronize()
-                times.append(e0.elapsed_time(e1))
-                acc_times.append(e0.elapsed_time(em))
-            res[name] = statistics.median(times[-args.steps:]) if prec == S.F32 else times[-1]
-            res[name + "_acc"] = statistics.median(acc_times[-args.steps:]) if prec == S.F32 else acc_times[-1]
-            res[name + "_r2"] = float(lev.r2.double().median().item())
-        acc_bytes = W * H * SPP * (G + 3) * 4
-        acc_gbs = acc_bytes / (res["f32_acc"] / 1e3) / 1e9
-        hbm_peak, peak_source = hbm_peak_gbs()
-        # DRAM bytes per launch from one ncu capture of lev_tma_f32 at 480x272, 64 spp:
-        # 406.1 MB read + 58.7 MB written, of which the per-pixel state is 58.7 MB each
-        # way (scaled by pixels) and the rest sample planes (scaled by pixel-samples).
-        state_b, samp_b = 58.726656e6, 406.123520e6 - 58.726656e6
-        traffic = (2 * state_b * (W * H) / (480 * 272) + samp_b * (W * H * SPP) / (480 * 272 * 64)) / 1e9
-        line = {"metric": "Mpix/s LEV regression (1080p, 512 spp, 7 features)", "value": W * H / res["f32"] / 1e3,
-                "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["f32"],
+        W, H, SPP = args.width or 1920, args.height or 1080, args.spp or 512
+        r = measure_lev(S, W, H, SPP, args.steps, args.warmup, with_plain=True)
+        line = {"metric": "Mpix/s LEV regression (1080p, 512 spp, 7 features)", "value": r["value"],
+                "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (compensated) + f64 solve",
                 "data": "synthetic (seeded, radiance linear in the features, target R^2 0.6)",
-                "config": {"workload": f"{W}x{H}, {SPP} spp, ridge lambda 1e-6, samples resident in HBM "
-                                       f"({W * H * SPP * (5 + G) * 4 / 1e9:.1f} GB of planes, "
-                                       f"{acc_bytes / 1e9:.1f} GB read by the regression)"},
-                "stage_ms": {"accumulate": res["f32_acc"], "solve": res["f32"] - res["f32_acc"]},
-                "roofline": {"kernel": "lev_tma_f32", "bound": "hbm", "achieved": acc_gbs, "peak": hbm_peak,
-                             "unit": "GB/s", "frac": acc_gbs / hbm_peak, "traffic": traffic,
-                             "algorithmic_gb": acc_bytes / 1e9, "peak_source": peak_source},
-                "median_r2": res["f32_r2"], "plain_f64": {"ms_per_step": res["f64"], "median_r2": res["f64_r2"]},
-                "speedup_vs_plain_f64": res["f64"] / res["f32"]}
+                "config": {"workload": r["workload"]}, "stage_ms": r["stage_ms"], "roofline": r["roofline"],
+                "median_r2": r["median_r2"], "plain_f64": r["plain_f64"],
+                "speedup_vs_plain_f64": r["speedup_vs_plain_f64"], "clocks": r["clocks"]}
     if rank == 0 and line is not None:
         print(json.dumps(line), flush=True)
 
@@ -729,6 +857,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the compact LEV / adaptive / serving legs")
+    ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the compact serving leg")
     ap.add_argument("--config", default="denoise", choices=["denoise", "serving", "adaptive", "lev"])
     ap.add_argument("--rate", type=float, default=10.0, help="serving: job arrivals per second")
     ap.add_argument("--rates", default="10,50,200,500", help="serving: comma-separated arrival rates to sweep")

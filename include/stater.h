@@ -343,6 +343,22 @@ stater_status stater_denoise_vars_pitched(const stater_denoise_vars_args *a, con
 stater_status stater_denoise_film_pitched(const stater_denoise_film_args *a, const stater_pitched_layout *layout,
                                           stater_stream stream);
 
+/* Tile-height autotuner of the FP32 window filters (no counterpart in the
+ * reference, whose filters have fixed launch shapes). The first FP32
+ * denoiseVars / denoiseFilm call of each shape class (filter, transform count,
+ * radius, feature use, image-size class: up to 2^18, 2^20 or more pixels) on a
+ * device times the row-ring kernels at tile heights 4, 8 and 16 rows, where the
+ * ring fits in shared memory, on its own stream, synchronising it once, and
+ * keeps the fastest for later calls. Results are bitwise the same at every
+ * height. Calls on a stream being captured into a CUDA graph use the default
+ * height and tune nothing. enable = 0 switches tuning off and forgets the
+ * choices (all calls then use the default); 1 switches it back on. */
+stater_status stater_set_autotune(int32_t enable);
+/* The tile height chosen for a shape class on the current device (filter 0 =
+ * denoiseVars, 1 = denoiseFilm), or 0 if none has been tuned yet. */
+int32_t stater_tuned_tile_height(int32_t filter, int32_t n_transforms, int32_t width, int32_t height,
+                                 int32_t filter_radius);
+
 /* A test order for stater_denoise_film_args.test_order: the most compressing
  * transforms first (asinh, cbrt and Box-Cox with lambda < 1/2, sqrt, log1p,
  * other Box-Cox), the untransformed set (transform 0) last; they reject most
@@ -458,6 +474,39 @@ stater_status stater_lev_accumulate(int32_t width, int32_t height, int32_t n_fea
 stater_status stater_lev_solve(int32_t width, int32_t height, int32_t n_features,
                                stater_precision precision, const void *state, double lambda,
                                void *beta, void *m2C, void *r2, stater_stream stream);
+
+/* ---- batches: many images through one launch per stage ----------------- */
+
+/* No counterpart in the reference, which makes one call per image per stage
+ * (statpath.cpp:424-441). A batch takes, per image, the arguments of the calls
+ * a caller would make for it (stater_accumulate with the film sums,
+ * stater_film_update_image into film_rgb, stater_denoise_vars,
+ * stater_denoise_film with film = film_rgb) and runs them together: the
+ * accumulations and film images per image, then every denoise stage as one
+ * launch over the tiles of all images that share a kernel form (transform-count
+ * class, moment/LEV variant, multi-transform mode, radius). Each image's
+ * outputs are bitwise those of its own calls. FP32 form only (STATER_F32,
+ * STATER_ACC_FAST), up to 5 transforms and 7 range-kernel feature channels per
+ * image, no pixel index, no accept bits.
+ * The first stater_batch_run tunes each launch's tile height on the data (one
+ * synchronisation of the stream) and records the sequence into a CUDA graph,
+ * so later runs are one graph launch; it must not itself be captured. The
+ * batch keeps the pointers it was given: every buffer must stay allocated, at
+ * the same address, until stater_batch_destroy. With reset = 1 each run first
+ * zeroes each image's n, statistics, feature means and film sums (a fresh
+ * image per run); with 0 the runs keep adding samples like repeated calls. */
+typedef struct {
+    stater_accumulate_args acc;
+    float *film_rgb;            /* [3][W*H]: Film::UpdateImage of the job's film sums */
+    float film_scale;
+    stater_denoise_vars_args vars;
+    stater_denoise_film_args film;
+} stater_batch_job;
+typedef struct stater_batch stater_batch;
+stater_status stater_batch_create(const stater_batch_job *jobs, int32_t n_jobs, int32_t reset, stater_batch **out);
+stater_status stater_batch_run(stater_batch *batch, stater_stream stream);
+/* Waits for the device, then frees the batch's tables and graph. */
+stater_status stater_batch_destroy(stater_batch *batch);
 
 /* ---- serving: continuous batching of denoise jobs ---------------------- */
 

@@ -84,6 +84,11 @@ class TargetSppArgs(C.Structure):
                 ("tmax", C.c_int32), ("as_source", C.c_int32), ("targetspp", VP)]
 
 
+class BatchJob(C.Structure):
+    _fields_ = [("acc", AccumulateArgs), ("film_rgb", VP), ("film_scale", C.c_float), ("vars", DenoiseVarsArgs),
+                ("film", DenoiseFilmArgs)]
+
+
 class PitchedLayout(C.Structure):
     _fields_ = [("rgb_step", C.c_int64), ("scalar_step", C.c_int64), ("n_step", C.c_int64)]
 
@@ -141,6 +146,11 @@ def load() -> C.CDLL:
         "stater_calc_mean_var": (st, [C.c_int32, C.c_int32, VP, VP, VP, VP]),
         "stater_film_add_samples": (st, [C.POINTER(FilmArgs), VP]),
         "stater_test_order": (st, [C.POINTER(Transform), C.c_int32, VP]),
+        "stater_set_autotune": (st, [C.c_int32]),
+        "stater_batch_create": (st, [C.POINTER(BatchJob), C.c_int32, C.c_int32, C.POINTER(VP)]),
+        "stater_batch_run": (st, [VP, VP]),
+        "stater_batch_destroy": (st, [VP]),
+        "stater_tuned_tile_height": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
         "stater_film_update_image": (st, [C.c_int32, C.c_int32, VP, VP, VP, C.c_float, VP, VP]),
         "stater_lev_state_size": (C.c_int32, [C.c_int32, C.c_int32]),
         "stater_lev_accumulate": (st, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, VP, VP, C.c_int32, VP, VP]),

@@ -130,6 +130,11 @@ class StatBuffers:
                 raise ValueError("with pixel_index the samples are [S, 5+G, N]")
         elif samples.shape[1:] != (5 + self.G, self.H, self.W):
             raise ValueError(f"samples shape {tuple(samples.shape)} does not match the buffers")
+        a = self._acc_args(samples, count, mode, film, pixel_index)
+        L.call("stater_accumulate", C.byref(a), _stream_ptr(stream))
+
+    def _acc_args(self, samples, count, mode, film, pixel_index=None) -> L.AccumulateArgs:
+        S = samples.shape[0]
         a = L.AccumulateArgs()
         a.width, a.height, a.n_samples, a.n_features = self.W, self.H, S, self.G
         a.samples, a.count = _ptr(samples), _ptr(count)
@@ -146,12 +151,17 @@ class StatBuffers:
                 raise ValueError("film geometry does not match the buffers")
             a.film_contrib_sum, a.film_weight_sum = _ptr(film.contrib_sum), _ptr(film.weight_sum)
             a.film_spill, a.film_max_sample_luminance = _ptr(film.spill), film.max_sample_luminance
-        L.call("stater_accumulate", C.byref(a), _stream_ptr(stream))
+        return a
 
     # -- stage 2 -----------------------------------------------------------------
     def denoise_vars(self, radius: int = 10, filter_sd: float = 10.0, var_z: float = 2.80703,
                      gbuffers: Sequence[GBufferSpec] = GBUFFERS_ALBEDO_NORMAL,
                      m2c_in: Optional[torch.Tensor] = None, stream=None) -> None:
+        a = self._vars_args(radius, filter_sd, var_z, gbuffers, m2c_in)
+        L.call("stater_denoise_vars", C.byref(a), _stream_ptr(stream))
+
+    def _vars_args(self, radius=10, filter_sd=10.0, var_z=2.80703, gbuffers=GBUFFERS_ALBEDO_NORMAL,
+                   m2c_in=None) -> L.DenoiseVarsArgs:
         a = L.DenoiseVarsArgs()
         a.n_buffers, a.width, a.height = self.K, self.W, self.H
         a.filter_radius, a.ds_factor, a.var_z = int(radius), -0.5 / (filter_sd * filter_sd), float(var_z)
@@ -170,7 +180,7 @@ class StatBuffers:
             a.varCD[k] = _ptr(self.varCD[k])
         a.m2C_in = _ptr(m2c_in)
         a.gbuffers = self._gbuffers(gbuffers)
-        L.call("stater_denoise_vars", C.byref(a), _stream_ptr(stream))
+        return a
 
     def denoise_film(self, radius: int = 10, filter_sd: float = 10.0, alpha: float = 0.01,
                      gbuffers: Sequence[GBufferSpec] = GBUFFERS_ALBEDO_NORMAL, mt_mode: int = L.MT_ALL,
@@ -180,6 +190,11 @@ class StatBuffers:
         "M" variant): the Welch discriminator uses each pixel's own sample
         variance (m2, or the LEV-corrected m2C with use_levc) instead of the
         denoised variance of denoise_vars."""
+        a = self._film_args(radius, filter_sd, alpha, gbuffers, mt_mode, use_levc, film, accept_bits, cascade)
+        L.call("stater_denoise_film", C.byref(a), _stream_ptr(stream))
+
+    def _film_args(self, radius=10, filter_sd=10.0, alpha=0.01, gbuffers=GBUFFERS_ALBEDO_NORMAL, mt_mode=L.MT_ALL,
+                   use_levc=False, film=None, accept_bits=None, cascade=True) -> L.DenoiseFilmArgs:
         a = L.DenoiseFilmArgs()
         a.n_buffers, a.width, a.height = self.K, self.W, self.H
         a.filter_radius, a.ds_factor, a.alpha = int(radius), -0.5 / (filter_sd * filter_sd), float(alpha)
@@ -202,7 +217,7 @@ class StatBuffers:
         for k, (kind, lam) in enumerate(self.transforms):
             tr[k].kind, tr[k].lambda_ = kind, lam
         L.call("stater_test_order", tr, self.K, C.cast(a.test_order, C.c_void_p))
-        L.call("stater_denoise_film", C.byref(a), _stream_ptr(stream))
+        return a
 
     def calc_target_spp(self, spp: int, out: torch.Tensor, relative: bool = True, eps: float = 1e-4,
                         tmin: int = 16, tmax: int = 1024, as_source: int = L.AS_DENOISED, stream=None) -> None:
@@ -327,6 +342,51 @@ class LevState:
     def solve(self, lam: float = 1e-6, stream=None) -> None:
         L.call("stater_lev_solve", self.W, self.H, self.G, self.precision, _ptr(self.state), float(lam),
                _ptr(self.beta), _ptr(self.m2C), _ptr(self.r2), _stream_ptr(stream))
+
+
+class Batch:
+    """Several images through one launch per denoise stage (stater_batch_*).
+
+    Each job is a dict with `buffers` (an FP32 StatBuffers), `film` (its Film),
+    `samples` (planes [S, 5+G, H, W]) and optionally `count`, `radius`,
+    `filter_sd`, `alpha`, `var_z`, `gbuffers` (both filters), `mt_mode`,
+    `use_levc`, `cascade`. One run accumulates every job's samples (with the film
+    sums), makes its film image and runs denoise_vars and denoise_film, each
+    image giving the same bits as those calls made one by one. With reset=True
+    every run starts from zeroed statistics and film sums. The first run tunes
+    and records a CUDA graph; later runs replay it. The buffers must outlive the
+    batch."""
+
+    def __init__(self, jobs, reset: bool = True):
+        arr = (L.BatchJob * len(jobs))()
+        for i, j in enumerate(jobs):
+            b, film = j["buffers"], j["film"]
+            if b.precision != L.F32:
+                raise ValueError("a batch runs the FP32 form")
+            g = j.get("gbuffers", GBUFFERS_ALBEDO_NORMAL)
+            R, sd = j.get("radius", 10), j.get("filter_sd", 10.0)
+            arr[i].acc = b._acc_args(j["samples"], j.get("count"), L.ACC_FAST, film)
+            arr[i].film_rgb, arr[i].film_scale = _ptr(film.rgb), film.scale
+            arr[i].vars = b._vars_args(R, sd, j.get("var_z", 2.80703), g)
+            arr[i].film = b._film_args(R, sd, j.get("alpha", 0.01), g, j.get("mt_mode", L.MT_ALL),
+                                       j.get("use_levc", False), film.rgb, None, j.get("cascade", True))
+        self._jobs = list(jobs)
+        self._h = C.c_void_p()
+        L.call("stater_batch_create", arr, len(jobs), int(bool(reset)), C.byref(self._h))
+
+    def run(self, stream=None) -> None:
+        L.call("stater_batch_run", self._h, _stream_ptr(stream))
+
+    def close(self) -> None:
+        if self._h:
+            L.call("stater_batch_destroy", self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def setup() -> None:

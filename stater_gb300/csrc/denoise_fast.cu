@@ -15,9 +15,13 @@
 //    per-pair bounds (tables indexed by integer df) and only the narrow band
 //    between them evaluates the exact df and the interpolated quantile. The
 //    exact branch falls back to FP64 when the summed variance is near zero.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <map>
+#include <tuple>
 #include <vector>
 
 #include "denoise_params.cuh"
@@ -95,10 +99,8 @@ struct FastFilm {
 // ---------------------------------------------------------------------------
 // Per-pixel variance statistics.
 // ---------------------------------------------------------------------------
-__global__ void vars_stats_f32(FastVars P) {
+__device__ __forceinline__ void vars_stats_body(const FastVars &P, size_t p, int k) {
     const size_t HW = (size_t)P.W * P.H;
-    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int k = blockIdx.y;
     if (p >= HW) return;
     const int nn = P.n[p];
     const float n = (float)nn;
@@ -142,6 +144,10 @@ __global__ void vars_stats_f32(FastVars P) {
         }
     }
     P.jb[k][p] = nn < 2 ? 0.f : jbsum;
+}
+
+__global__ void vars_stats_f32(FastVars P) {
+    vars_stats_body(P, (size_t)blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 __device__ __forceinline__ void load_penalty(float *dst, const int32_t *__restrict__ n, int W, int H, int x0,
@@ -326,10 +332,8 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P)
     }
 }
 
-__global__ void film_discr_f32(FastFilm P) {
+__device__ __forceinline__ void film_discr_body(const FastFilm &P, size_t p, int k) {
     const size_t HW = (size_t)P.W * P.H;
-    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int k = blockIdx.y;
     if (p >= HW) return;
     const int nn = P.n[p];
 #pragma unroll
@@ -339,6 +343,10 @@ __global__ void film_discr_f32(FastFilm P) {
         const float v = P.discr_source == STATER_DISCR_SAMPLE ? P.var[k][o] / ((float)nn - 1.f) : P.var[k][o];
         P.discr[k][o] = nn < 2 ? 0.f : v / (float)nn;
     }
+}
+
+__global__ void film_discr_f32(FastFilm P) {
+    film_discr_body(P, (size_t)blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 __device__ __forceinline__ float lut_interp_f32(const float *lut, int N, float u) {
@@ -715,14 +723,14 @@ __device__ __forceinline__ void ring_store(const float4 (&pend)[kRingPer], float
 }
 
 template <bool LEVC, bool ZPIX, int KMAX, int TY>
-__global__ void __launch_bounds__(kTX2 *TY) vars_ring_f32(FastVars P) {
+__device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by) {
     constexpr int TW = VarsRing<LEVC, ZPIX>::TW;
     constexpr int NS = TY + 1;
     extern __shared__ float4 ring[];
     const int R = P.R, hw = kTX2 + 2 * R, hh = TY + 2 * R;
     const int K = P.K, nf = P.feat.nch;
     const int nrec = kRingFW + K * TW;
-    const int x0 = blockIdx.x * kTX2, y0 = blockIdx.y * TY;
+    const int x0 = bx * kTX2, y0 = by * TY;
     const int lx = threadIdx.x % kTX2, tr = threadIdx.x / kTX2;
     const int x = x0 + lx, y = y0 + tr;
     const bool in = x < P.W && y < P.H;
@@ -808,6 +816,11 @@ __global__ void __launch_bounds__(kTX2 *TY) vars_ring_f32(FastVars P) {
     }
 }
 
+template <bool LEVC, bool ZPIX, int KMAX, int TY>
+__global__ void __launch_bounds__(kTX2 *TY) vars_ring_f32(FastVars P) {
+    vars_ring_body<LEVC, ZPIX, KMAX, TY>(P, blockIdx.x, blockIdx.y);
+}
+
 // Film ring fields: features with n (as float) in field 7, {film x3, 0}, and per
 // transform {mean x3, discr_0}, {discr_1, discr_2, 0, 0}.
 __device__ __forceinline__ float4 film_ring_value(const FastFilm &P, int rec, int col, int hrow, int x0, int y0) {
@@ -851,14 +864,14 @@ __device__ __forceinline__ float4 film_ring_value(const FastFilm &P, int rec, in
 // same order (rows, then dx), so filmD is bitwise that of the per-transform
 // kernel.
 template <int KMAX, int TY, bool JB>
-__global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
+__device__ __forceinline__ void film_ring_body(const FastFilm &P, int bx, int by) {
     constexpr int NS = TY + 1;
     extern __shared__ float4 ring[];
     __shared__ int s_nmin, s_nmax;
     const int R = P.R, hw = kTX2 + 2 * R, hh = TY + 2 * R;
     const int K = P.K, nf = P.feat.nch;
     const int nrec = kRingFW + 1 + 2 * K;
-    const int x0 = blockIdx.x * kTX2, y0 = blockIdx.y * TY;
+    const int x0 = bx * kTX2, y0 = by * TY;
     const int t = threadIdx.x, lx = t % kTX2, tr = t / kTX2;
     const int x = x0 + lx, y = y0 + tr;
     const bool in = x < P.W && y < P.H;
@@ -1067,6 +1080,11 @@ __global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
     for (int c = 0; c < 3; c++) P.filmD[(size_t)c * HW + gi] = sf[c] / sw;
 }
 
+template <int KMAX, int TY, bool JB>
+__global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_f32(FastFilm P) {
+    film_ring_body<KMAX, TY, JB>(P, blockIdx.x, blockIdx.y);
+}
+
 // ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
@@ -1148,6 +1166,89 @@ int ring_ty(int R, int nrec) {
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Tile-height autotuner of the row-ring filters. The tile height TY trades the
+// halo rows a CTA streams per output row ((TY + 2R) / TY) against occupancy (a
+// TY = 16 ring takes one CTA per SM; TY = 4 and 8 take two). The best choice
+// depends on the radius, the transform count and the image size (small images
+// have few tiles per SM), so the first call of each shape class times every
+// height whose ring fits in shared memory (4, 8, 16), with CUDA events on the
+// call's own stream, and caches the fastest per device. Results do not depend
+// on TY (every pixel sums its neighbours in the same order), so tuning changes
+// speed only. Calls made while their stream is being captured into a graph,
+// or with the autotuner switched off (stater_set_autotune), use the default
+// height (8 where two CTAs fit per SM, else 4).
+// ---------------------------------------------------------------------------
+struct TuneKey {
+    int dev, filter, km, nrec, R, variant, size_class;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(dev, filter, km, nrec, R, variant, size_class) <
+               std::tie(o.dev, o.filter, o.km, o.nrec, o.R, o.variant, o.size_class);
+    }
+};
+std::mutex g_tune_mutex;
+std::map<TuneKey, int> g_tuned;
+std::atomic<int> g_autotune{1};
+
+int size_class(size_t px) { return px <= ((size_t)1 << 18) ? 0 : px <= ((size_t)1 << 20) ? 1 : 2; }
+
+bool ring_fits(int R, int nrec, int ty) { return ring_smem(R, nrec, ty) <= kSmemLimit; }
+
+bool stream_capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &st) != cudaSuccess) {
+        cudaGetLastError();
+        return true;  // cannot tell: do not synchronise
+    }
+    return st != cudaStreamCaptureStatusNone;
+}
+
+// launch(ty) enqueues the filter with tile height ty on s and returns its error.
+template <typename LaunchFn>
+int pick_ring_ty(int filter, int km, int nrec, int R, int variant, size_t px, cudaStream_t s, LaunchFn launch) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const TuneKey key{dev, filter, km, nrec, R, variant, size_class(px)};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mutex);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) return it->second;
+    }
+    const int def = ring_ty(R, nrec);
+    if (!g_autotune.load() || stream_capturing(s)) return def;
+    int cands[3], nc = 0;
+    for (int ty : {4, 8, 16})
+        if (ring_fits(R, nrec, ty)) cands[nc++] = ty;
+    int best = def;
+    if (nc > 1) {
+        float best_ms = 1e30f;
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        for (int i = 0; i < nc; i++) {
+            if (launch(cands[i]) != cudaSuccess) {  // warm-up (shared-memory attribute, caches)
+                cudaGetLastError();
+                continue;
+            }
+            cudaEventRecord(e0, s);
+            launch(cands[i]);
+            cudaEventRecord(e1, s);
+            float ms = 1e30f;
+            if (cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+            cudaGetLastError();
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = cands[i];
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    g_tuned[key] = best;
+    return best;
+}
+
 template <typename KernelT>
 cudaError_t set_smem(KernelT kern, size_t bytes) {
     return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -1169,8 +1270,9 @@ void df_tables_release(int dev) {
     }
 }
 
-stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s) {
-    FastVars P;
+// Kernel parameters of one FP32 denoiseVars call (scratch pointers s2 / s2c
+// left to the caller).
+stater_status fill_fast_vars(const stater_denoise_vars_args *a, FastVars &P) {
     P.W = a->width;
     P.H = a->height;
     P.K = a->n_buffers;
@@ -1195,9 +1297,17 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
         P.varCD[k] = (float *)a->varCD[k];
     }
     P.m2c_in = (const float *)a->m2C_in;
-    const size_t HW = (size_t)P.W * P.H;
-    if (!make_featset(P.feat, a->gbuffers, HW))
+    P.s2 = P.s2c = nullptr;
+    if (!make_featset(P.feat, a->gbuffers, (size_t)P.W * P.H))
         return set_error(STATER_ERR_INVALID, "stater_denoise_vars: bad gbuffers (at most 24 channels, dr_factor <= 0)");
+    return STATER_OK;
+}
+
+stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s) {
+    FastVars P;
+    stater_status st = fill_fast_vars(a, P);
+    if (st != STATER_OK) return st;
+    const size_t HW = (size_t)P.W * P.H;
     float *scr = (float *)scratch(0, sizeof(float) * 2 * 3 * P.K * HW, s);
     if (!scr) return set_error(STATER_ERR_NOMEM, "stater_denoise_vars: scratch allocation failed");
     P.s2 = scr;
@@ -1211,11 +1321,11 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
     {
         const int km = ring_kmax(P.K);
         const int nrec = kRingFW + P.K * ((P.levc || !zp) ? 3 : 2);
-        const int ty = ring_ty(P.R, nrec);
-        if (km > 0 && ty > 0 && P.feat.nch <= kRingMF) {
-            const size_t sm = ring_smem(P.R, nrec, ty);
-            dim3 grid((P.W + kTX2 - 1) / kTX2, (P.H + ty - 1) / ty);
-            cudaError_t e = cudaErrorInvalidValue;
+        if (km > 0 && ring_ty(P.R, nrec) > 0 && P.feat.nch <= kRingMF) {
+            auto launch = [&](int ty) {
+                const size_t sm = ring_smem(P.R, nrec, ty);
+                dim3 grid((P.W + kTX2 - 1) / kTX2, (P.H + ty - 1) / ty);
+                cudaError_t e = cudaErrorInvalidValue;
 #define STATER_RING_VARS(LV, ZV, KV, TV)                                                   \
     if ((P.levc != 0) == LV && zp == ZV && km == KV && ty == TV) {                          \
         e = set_smem(vars_ring_f32<LV, ZV, KV, TV>, sm);                                    \
@@ -1226,13 +1336,18 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
 #define STATER_RING_VARS_T(TV)                                                                   \
     STATER_RING_VARS_K(true, true, TV) STATER_RING_VARS_K(true, false, TV)                        \
     STATER_RING_VARS_K(false, true, TV) STATER_RING_VARS_K(false, false, TV)
-            STATER_RING_VARS_T(8)
-            STATER_RING_VARS_T(4)
+                STATER_RING_VARS_T(16)
+                STATER_RING_VARS_T(8)
+                STATER_RING_VARS_T(4)
 #undef STATER_RING_VARS_T
 #undef STATER_RING_VARS_K
 #undef STATER_RING_VARS
-            if (e != cudaSuccess) return cuda_status(e, "vars_ring_f32 smem attribute");
-            STATER_CHECK_LAUNCH("vars_ring_f32");
+                return e == cudaSuccess ? cudaGetLastError() : e;
+            };
+            const int variant = (P.levc ? 1 : 0) + (zp ? 2 : 0) + (P.feat.nch > 0 ? 4 : 0);
+            const int ty = pick_ring_ty(0, km, nrec, P.R, variant, HW, s, launch);
+            cudaError_t e = launch(ty);
+            if (e != cudaSuccess) return cuda_status(e, "vars_ring_f32");
             return STATER_OK;
         }
     }
@@ -1267,8 +1382,8 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
     return STATER_OK;
 }
 
-stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s) {
-    FastFilm P;
+// Kernel parameters of one FP32 denoiseFilm call, tables included.
+stater_status fill_fast_film(const stater_denoise_film_args *a, FastFilm &P, cudaStream_t s) {
     P.W = a->width;
     P.H = a->height;
     P.K = a->n_buffers;
@@ -1312,6 +1427,14 @@ stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s
     P.tlo = dt->lo;
     P.thi = dt->hi;
     P.z2lo = dt->z2lo;
+    return STATER_OK;
+}
+
+stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s) {
+    FastFilm P;
+    stater_status st = fill_fast_film(a, P, s);
+    if (st != STATER_OK) return st;
+    const size_t HW = (size_t)P.W * P.H;
 
     dim3 g1((unsigned)((HW + 127) / 128), P.K);
     film_discr_f32<<<g1, 128, 0, s>>>(P);
@@ -1320,24 +1443,28 @@ stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s
     {
         const int km = ring_kmax(P.K);
         const int nrec = kRingFW + 1 + 2 * P.K;
-        const int ty = ring_ty(P.R, nrec);
-        if (km > 0 && ty > 0 && P.feat.nch <= kRingMF && !P.bits) {
-            const size_t sm = ring_smem(P.R, nrec, ty);
-            dim3 grid((P.W + kTX2 - 1) / kTX2, (P.H + ty - 1) / ty);
-            cudaError_t e = cudaErrorInvalidValue;
+        if (km > 0 && ring_ty(P.R, nrec) > 0 && P.feat.nch <= kRingMF && !P.bits) {
             const bool jb = P.mt_mode == STATER_MT_JB;
+            auto launch = [&](int ty) {
+                const size_t sm = ring_smem(P.R, nrec, ty);
+                dim3 grid((P.W + kTX2 - 1) / kTX2, (P.H + ty - 1) / ty);
+                cudaError_t e = cudaErrorInvalidValue;
 #define STATER_RING_FILM(KV, TV, JV)                                                          \
     if (km == KV && ty == TV && jb == JV) {                                                    \
         e = set_smem(film_ring_f32<KV, TV, JV>, sm);                                           \
         if (e == cudaSuccess) film_ring_f32<KV, TV, JV><<<grid, kTX2 * TV, sm, s>>>(P);        \
     }
-            STATER_RING_FILM(1, 8, false) STATER_RING_FILM(3, 8, false) STATER_RING_FILM(5, 8, false)
-            STATER_RING_FILM(1, 4, false) STATER_RING_FILM(3, 4, false) STATER_RING_FILM(5, 4, false)
-            STATER_RING_FILM(1, 8, true) STATER_RING_FILM(3, 8, true) STATER_RING_FILM(5, 8, true)
-            STATER_RING_FILM(1, 4, true) STATER_RING_FILM(3, 4, true) STATER_RING_FILM(5, 4, true)
+#define STATER_RING_FILM_T(TV, JV) STATER_RING_FILM(1, TV, JV) STATER_RING_FILM(3, TV, JV) STATER_RING_FILM(5, TV, JV)
+                STATER_RING_FILM_T(16, false) STATER_RING_FILM_T(8, false) STATER_RING_FILM_T(4, false)
+                STATER_RING_FILM_T(16, true) STATER_RING_FILM_T(8, true) STATER_RING_FILM_T(4, true)
+#undef STATER_RING_FILM_T
 #undef STATER_RING_FILM
-            if (e != cudaSuccess) return cuda_status(e, "film_ring_f32 smem attribute");
-            STATER_CHECK_LAUNCH("film_ring_f32");
+                return e == cudaSuccess ? cudaGetLastError() : e;
+            };
+            const int variant = (jb ? 1 : 0) + (P.feat.nch > 0 ? 4 : 0);
+            const int ty = pick_ring_ty(1, km, nrec, P.R, variant, HW, s, launch);
+            cudaError_t e = launch(ty);
+            if (e != cudaSuccess) return cuda_status(e, "film_ring_f32");
             return STATER_OK;
         }
     }
@@ -1368,6 +1495,33 @@ stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s
 }
 
 }  // namespace stater
+
+extern "C" stater_status stater_set_autotune(int32_t enable) {
+    using namespace stater;
+    clear_error();
+    if (enable != 0 && enable != 1) return set_error(STATER_ERR_INVALID, "stater_set_autotune: 0 or 1");
+    g_autotune.store(enable);
+    if (!enable) {
+        std::lock_guard<std::mutex> lk(g_tune_mutex);
+        g_tuned.clear();
+    }
+    return STATER_OK;
+}
+
+extern "C" int32_t stater_tuned_tile_height(int32_t filter, int32_t n_transforms, int32_t width, int32_t height,
+                                            int32_t filter_radius) {
+    using namespace stater;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int km = ring_kmax(n_transforms);
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    for (const auto &kv : g_tuned)
+        if (kv.first.dev == dev && kv.first.filter == filter && kv.first.km == km && kv.first.R == filter_radius &&
+            kv.first.size_class == size_class((size_t)width * height) &&
+            kv.first.nrec == (filter == 1 ? kRingFW + 1 + 2 * n_transforms : kv.first.nrec))
+            return kv.second;
+    return 0;
+}
 
 extern "C" stater_status stater_test_order(const stater_transform *transforms, int32_t n_transforms,
                                            int32_t *order) {
@@ -1405,3 +1559,383 @@ extern "C" stater_status stater_test_order(const stater_transform *transforms, i
     return STATER_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Batches: many small images through one launch per stage.
+//
+// A small image (256x256 is 2,048 ring tiles of 32x8) fills a fraction of the
+// GPU and pays a launch and a tail per stage. A batch runs the jobs' stages
+// together: every job's accumulation (with the film sums) and film image on
+// one stream, then each denoise stage as ONE launch covering the tiles of all
+// jobs that share a kernel instantiation (transform-count class, LEV / moment
+// variant, multi-transform mode, radius): a CTA finds its job by binary search
+// over the per-job tile offsets and runs the same tile code as the
+// single-image kernels, so each job's results are bitwise those of its
+// single-image calls. The first run of a batch tunes each class's tile height
+// on the real data and then records the whole sequence into a CUDA graph;
+// later runs replay the graph (one launch for the host).
+// ---------------------------------------------------------------------------
+namespace stater {
+namespace {
+
+__device__ __forceinline__ int batch_job(const int *__restrict__ start, int njobs, int t) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(start + mid) <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// start[j]: first block of job j (blocks of 128 pixels), start[njobs] = total
+__global__ void vars_stats_batch(const FastVars *__restrict__ jobs, const int *__restrict__ start, int njobs) {
+    const int j = batch_job(start, njobs, blockIdx.x);
+    const FastVars &P = jobs[j];
+    if ((int)blockIdx.y >= P.K) return;
+    vars_stats_body(P, (size_t)(blockIdx.x - __ldg(start + j)) * blockDim.x + threadIdx.x, blockIdx.y);
+}
+
+__global__ void film_discr_batch(const FastFilm *__restrict__ jobs, const int *__restrict__ start, int njobs) {
+    const int j = batch_job(start, njobs, blockIdx.x);
+    const FastFilm &P = jobs[j];
+    if ((int)blockIdx.y >= P.K) return;
+    film_discr_body(P, (size_t)(blockIdx.x - __ldg(start + j)) * blockDim.x + threadIdx.x, blockIdx.y);
+}
+
+// jobs: the class's jobs only; start[j]: first ring tile of job j
+template <bool LEVC, bool ZPIX, int KMAX, int TY>
+__global__ void __launch_bounds__(kTX2 *TY) vars_ring_batch(const FastVars *__restrict__ jobs,
+                                                            const int *__restrict__ start, int njobs) {
+    const int j = batch_job(start, njobs, blockIdx.x);
+    const FastVars &P = jobs[j];
+    const int tx = (P.W + kTX2 - 1) / kTX2, local = blockIdx.x - __ldg(start + j);
+    vars_ring_body<LEVC, ZPIX, KMAX, TY>(P, local % tx, local / tx);
+}
+
+template <int KMAX, int TY, bool JB>
+__global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_batch(const FastFilm *__restrict__ jobs,
+                                                                    const int *__restrict__ start, int njobs) {
+    const int j = batch_job(start, njobs, blockIdx.x);
+    const FastFilm &P = jobs[j];
+    const int tx = (P.W + kTX2 - 1) / kTX2, local = blockIdx.x - __ldg(start + j);
+    film_ring_body<KMAX, TY, JB>(P, local % tx, local / tx);
+}
+
+// Jobs of one ring instantiation.
+struct RingClass {
+    int filter;      // 0: variance filter, 1: film filter
+    int km, nrec, R;
+    bool levc, zp, jb, feats;
+    std::vector<int> jobs;
+    int ty = 0;
+    int ntiles = 0;
+    void *d_params = nullptr;  // the class's FastVars / FastFilm blocks
+    int *d_start = nullptr;
+};
+
+}  // namespace
+}  // namespace stater
+
+struct stater_batch {
+    int dev = 0;
+    int reset = 0;
+    std::vector<stater_batch_job> jobs;
+    std::vector<stater::FastVars> vars;
+    std::vector<stater::FastFilm> film;
+    std::vector<stater::RingClass> classes;
+    stater::FastVars *d_vars = nullptr;
+    stater::FastFilm *d_film = nullptr;
+    int *d_pix_start = nullptr;  // elementwise stages: blocks of 128 pixels per job
+    int pix_blocks = 0, kmax = 1;
+    float *s2 = nullptr;         // per job s2 / s2c planes
+    bool recorded = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t capture = nullptr;
+    bool ring_ok = true;
+};
+
+namespace stater {
+namespace {
+
+void batch_free(stater_batch *b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->capture) cudaStreamDestroy(b->capture);
+    for (auto &c : b->classes) {
+        cudaFree(c.d_params);
+        cudaFree(c.d_start);
+    }
+    cudaFree(b->d_vars);
+    cudaFree(b->d_film);
+    cudaFree(b->d_pix_start);
+    cudaFree(b->s2);
+}
+
+template <typename T>
+cudaError_t upload(T **dst, const T *src, size_t n) {
+    cudaError_t e = cudaMalloc(dst, sizeof(T) * (n ? n : 1));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice);
+}
+
+cudaError_t launch_ring_class(stater_batch *b, RingClass &c, int ty, cudaStream_t s) {
+    // per-job ring tile offsets at this height
+    std::vector<int> start;
+    int total = 0;
+    for (int j : c.jobs) {
+        start.push_back(total);
+        const int W = c.filter == 0 ? b->vars[j].W : b->film[j].W, H = c.filter == 0 ? b->vars[j].H : b->film[j].H;
+        total += ((W + kTX2 - 1) / kTX2) * ((H + ty - 1) / ty);
+    }
+    start.push_back(total);
+    if (c.ty != ty || !c.d_start) {
+        cudaFree(c.d_start);
+        c.d_start = nullptr;
+        cudaError_t e = upload(&c.d_start, start.data(), start.size());
+        if (e != cudaSuccess) return e;
+        c.ty = ty;
+        c.ntiles = total;
+    }
+    const size_t sm = ring_smem(c.R, c.nrec, ty);
+    const int nj = (int)c.jobs.size();
+    cudaError_t e = cudaErrorInvalidValue;
+    if (c.filter == 0) {
+        const FastVars *P = (const FastVars *)c.d_params;
+#define STATER_BATCH_VARS(LV, ZV, KV, TV)                                                                  \
+    if (c.levc == LV && c.zp == ZV && c.km == KV && ty == TV) {                                              \
+        e = set_smem(vars_ring_batch<LV, ZV, KV, TV>, sm);                                                   \
+        if (e == cudaSuccess) vars_ring_batch<LV, ZV, KV, TV><<<total, kTX2 * TV, sm, s>>>(P, c.d_start, nj); \
+    }
+#define STATER_BATCH_VARS_K(LV, ZV, TV) \
+    STATER_BATCH_VARS(LV, ZV, 1, TV) STATER_BATCH_VARS(LV, ZV, 3, TV) STATER_BATCH_VARS(LV, ZV, 5, TV)
+#define STATER_BATCH_VARS_T(TV)                                                       \
+    STATER_BATCH_VARS_K(true, true, TV) STATER_BATCH_VARS_K(true, false, TV)          \
+    STATER_BATCH_VARS_K(false, true, TV) STATER_BATCH_VARS_K(false, false, TV)
+        STATER_BATCH_VARS_T(16)
+        STATER_BATCH_VARS_T(8)
+        STATER_BATCH_VARS_T(4)
+#undef STATER_BATCH_VARS_T
+#undef STATER_BATCH_VARS_K
+#undef STATER_BATCH_VARS
+    } else {
+        const FastFilm *P = (const FastFilm *)c.d_params;
+#define STATER_BATCH_FILM(KV, TV, JV)                                                               \
+    if (c.km == KV && ty == TV && c.jb == JV) {                                                      \
+        e = set_smem(film_ring_batch<KV, TV, JV>, sm);                                               \
+        if (e == cudaSuccess) film_ring_batch<KV, TV, JV><<<total, kTX2 * TV, sm, s>>>(P, c.d_start, nj); \
+    }
+#define STATER_BATCH_FILM_T(TV, JV) STATER_BATCH_FILM(1, TV, JV) STATER_BATCH_FILM(3, TV, JV) STATER_BATCH_FILM(5, TV, JV)
+        STATER_BATCH_FILM_T(16, false) STATER_BATCH_FILM_T(8, false) STATER_BATCH_FILM_T(4, false)
+        STATER_BATCH_FILM_T(16, true) STATER_BATCH_FILM_T(8, true) STATER_BATCH_FILM_T(4, true)
+#undef STATER_BATCH_FILM_T
+#undef STATER_BATCH_FILM
+    }
+    return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+// Enqueues one run of the batch on s. tune: pick the classes' tile heights first.
+stater_status batch_enqueue(stater_batch *b, cudaStream_t s, bool tune) {
+    const int n = (int)b->jobs.size();
+    for (int j = 0; j < n; j++) {
+        const stater_batch_job &J = b->jobs[j];
+        const size_t HW = (size_t)J.acc.width * J.acc.height;
+        if (b->reset) {
+            cudaMemsetAsync(J.acc.n, 0, sizeof(int32_t) * HW, s);
+            cudaMemsetAsync(J.acc.stats, 0, sizeof(float) * (size_t)J.acc.n_transforms * STATER_NQ * 3 * HW, s);
+            if (J.acc.gmean && J.acc.n_features > 0)
+                cudaMemsetAsync(J.acc.gmean, 0, sizeof(float) * (size_t)J.acc.n_features * HW, s);
+            cudaMemsetAsync(J.acc.film_contrib_sum, 0, sizeof(float) * 3 * HW, s);
+            cudaMemsetAsync(J.acc.film_weight_sum, 0, sizeof(float) * HW, s);
+            cudaMemsetAsync(J.acc.film_spill, 0, sizeof(float) * 4 * HW, s);
+        }
+        stater_status st = stater_accumulate(&J.acc, (stater_stream)s);
+        if (st != STATER_OK) return st;
+        st = stater_film_update_image(J.acc.width, J.acc.height, J.acc.film_contrib_sum, J.acc.film_weight_sum,
+                                      J.acc.film_spill, J.film_scale, J.film_rgb, (stater_stream)s);
+        if (st != STATER_OK) return st;
+    }
+    {
+        dim3 g((unsigned)b->pix_blocks, (unsigned)b->kmax);
+        vars_stats_batch<<<g, 128, 0, s>>>(b->d_vars, b->d_pix_start, n);
+        STATER_CHECK_LAUNCH("vars_stats_batch");
+    }
+    for (int pass = 0; pass < 2; pass++) {
+        if (pass == 1) {
+            dim3 g((unsigned)b->pix_blocks, (unsigned)b->kmax);
+            film_discr_batch<<<g, 128, 0, s>>>(b->d_film, b->d_pix_start, n);
+            STATER_CHECK_LAUNCH("film_discr_batch");
+        }
+        for (auto &c : b->classes) {
+            if (c.filter != pass) continue;
+            int ty = c.ty;
+            if (tune || !ty) {
+                size_t px = 0;
+                for (int j : c.jobs) px += (size_t)b->jobs[j].acc.width * b->jobs[j].acc.height;
+                const int variant = 64 + (c.filter == 0 ? (c.levc ? 1 : 0) + (c.zp ? 2 : 0) : (c.jb ? 1 : 0)) +
+                                    (c.feats ? 4 : 0);
+                ty = pick_ring_ty(c.filter, c.km, c.nrec, c.R, variant, px, s,
+                                  [&](int t) { return launch_ring_class(b, c, t, s); });
+            }
+            cudaError_t e = launch_ring_class(b, c, ty, s);
+            if (e != cudaSuccess) return cuda_status(e, "batched ring filter");
+        }
+    }
+    return STATER_OK;
+}
+
+}  // namespace
+}  // namespace stater
+
+using namespace stater;
+
+extern "C" stater_status stater_batch_create(const stater_batch_job *jobs, int32_t n_jobs, int32_t reset,
+                                             stater_batch **out) {
+    clear_error();
+    if (!jobs || n_jobs < 1 || !out || (reset != 0 && reset != 1))
+        return set_error(STATER_ERR_INVALID, "stater_batch_create: bad arguments");
+    *out = nullptr;
+    auto *b = new stater_batch();
+    cudaGetDevice(&b->dev);
+    b->reset = reset;
+    b->jobs.assign(jobs, jobs + n_jobs);
+    auto fail = [&](stater_status st) {
+        batch_free(b);
+        delete b;
+        return st;
+    };
+    size_t s2_floats = 0;
+    std::vector<int> pix_start;
+    for (int j = 0; j < n_jobs; j++) {
+        const stater_batch_job &J = jobs[j];
+        const stater_accumulate_args &A = J.acc;
+        if (A.precision != STATER_F32 || A.mode != STATER_ACC_FAST || J.vars.precision != STATER_F32 ||
+            J.film.precision != STATER_F32)
+            return fail(set_error(STATER_ERR_INVALID, "stater_batch_create: a batch runs the FP32 form only"));
+        if (!A.film_contrib_sum || !J.film_rgb || A.pixel_index)
+            return fail(set_error(STATER_ERR_INVALID, "stater_batch_create: jobs need film sums, film_rgb and no "
+                                                      "pixel index"));
+        if (J.vars.width != A.width || J.vars.height != A.height || J.film.width != A.width ||
+            J.film.height != A.height || J.vars.n_buffers != A.n_transforms || J.film.n_buffers != A.n_transforms ||
+            J.film.accept_bits)
+            return fail(set_error(STATER_ERR_INVALID, "stater_batch_create: the stages of a job disagree"));
+        s2_floats += (size_t)2 * 3 * A.n_transforms * A.width * A.height;
+    }
+    cudaError_t ce = cudaMalloc(&b->s2, sizeof(float) * (s2_floats ? s2_floats : 1));
+    if (ce != cudaSuccess) return fail(cuda_status(ce, "stater_batch_create: scratch"));
+    b->vars.resize(n_jobs);
+    b->film.resize(n_jobs);
+    size_t off = 0;
+    int blocks = 0;
+    for (int j = 0; j < n_jobs; j++) {
+        const stater_batch_job &J = jobs[j];
+        stater_status st = fill_fast_vars(&J.vars, b->vars[j]);
+        if (st != STATER_OK) return fail(st);
+        st = fill_fast_film(&J.film, b->film[j], nullptr);
+        if (st != STATER_OK) return fail(st);
+        FastVars &V = b->vars[j];
+        const size_t HW = (size_t)V.W * V.H;
+        V.s2 = b->s2 + off;
+        V.s2c = V.s2 + (size_t)3 * V.K * HW;
+        off += (size_t)2 * 3 * V.K * HW;
+        pix_start.push_back(blocks);
+        blocks += (int)((HW + 127) / 128);
+        b->kmax = std::max(b->kmax, V.K);
+        // ring classes (jobs outside the ring kernels' range are not batched)
+        const bool zp = V.max_moment < 4;
+        const int kmv = ring_kmax(V.K), nrv = kRingFW + V.K * ((V.levc || !zp) ? 3 : 2);
+        const FastFilm &F = b->film[j];
+        const int nrf = kRingFW + 1 + 2 * F.K;
+        if (!(kmv > 0 && ring_ty(V.R, nrv) > 0 && V.feat.nch <= kRingMF && ring_ty(F.R, nrf) > 0 &&
+              F.feat.nch <= kRingMF))
+            return fail(set_error(STATER_ERR_UNSUPPORTED, "stater_batch_create: a job needs more than 5 transforms, "
+                                                          "7 feature channels or the ring's shared memory"));
+        for (int f = 0; f < 2; f++) {
+            RingClass key;
+            key.filter = f;
+            key.km = kmv;
+            key.nrec = f == 0 ? nrv : nrf;
+            key.R = f == 0 ? V.R : F.R;
+            key.levc = f == 0 && V.levc;
+            key.zp = f == 0 && zp;
+            key.jb = f == 1 && F.mt_mode == STATER_MT_JB;
+            key.feats = (f == 0 ? V.feat.nch : F.feat.nch) > 0;
+            RingClass *found = nullptr;
+            for (auto &c : b->classes)
+                if (c.filter == key.filter && c.km == key.km && c.nrec == key.nrec && c.R == key.R &&
+                    c.levc == key.levc && c.zp == key.zp && c.jb == key.jb && c.feats == key.feats)
+                    found = &c;
+            if (!found) {
+                b->classes.push_back(key);
+                found = &b->classes.back();
+            }
+            found->jobs.push_back(j);
+        }
+    }
+    pix_start.push_back(blocks);
+    b->pix_blocks = blocks;
+    if ((ce = upload(&b->d_vars, b->vars.data(), b->vars.size())) != cudaSuccess ||
+        (ce = upload(&b->d_film, b->film.data(), b->film.size())) != cudaSuccess ||
+        (ce = upload(&b->d_pix_start, pix_start.data(), pix_start.size())) != cudaSuccess)
+        return fail(cuda_status(ce, "stater_batch_create: job tables"));
+    for (auto &c : b->classes) {
+        std::vector<unsigned char> blob;
+        const size_t sz = c.filter == 0 ? sizeof(FastVars) : sizeof(FastFilm);
+        blob.resize(sz * c.jobs.size());
+        for (size_t i = 0; i < c.jobs.size(); i++)
+            std::memcpy(blob.data() + i * sz,
+                        c.filter == 0 ? (const void *)&b->vars[c.jobs[i]] : (const void *)&b->film[c.jobs[i]], sz);
+        if ((ce = cudaMalloc(&c.d_params, blob.size())) != cudaSuccess ||
+            (ce = cudaMemcpy(c.d_params, blob.data(), blob.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(cuda_status(ce, "stater_batch_create: class tables"));
+    }
+    *out = b;
+    return STATER_OK;
+}
+
+extern "C" stater_status stater_batch_run(stater_batch *b, stater_stream stream) {
+    clear_error();
+    if (!b) return set_error(STATER_ERR_INVALID, "stater_batch_run: null batch");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != b->dev) return set_error(STATER_ERR_INVALID, "stater_batch_run: the batch belongs to another device");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (b->exec) return cuda_status(cudaGraphLaunch(b->exec, s), "stater_batch_run: graph launch");
+    if (stream_capturing(s))
+        return set_error(STATER_ERR_INVALID, "stater_batch_run: the first run of a batch must not be captured");
+    // first run: eager, with the tile heights tuned on the real data, then the
+    // same sequence is recorded for the later runs
+    stater_status st = batch_enqueue(b, s, true);
+    if (st != STATER_OK) return st;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e, "stater_batch_run: capture stream");
+    e = cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_status(e, "stater_batch_run: begin capture");
+    st = batch_enqueue(b, b->capture, false);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(b->capture, &g);
+    if (st != STATER_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return cuda_status(e, "stater_batch_run: end capture");
+    b->graph = g;
+    e = cudaGraphInstantiate(&b->exec, g, 0);
+    if (e != cudaSuccess) {
+        b->exec = nullptr;
+        return cuda_status(e, "stater_batch_run: graph instantiate");
+    }
+    return STATER_OK;
+}
+
+extern "C" stater_status stater_batch_destroy(stater_batch *b) {
+    clear_error();
+    if (!b) return STATER_OK;
+    cudaDeviceSynchronize();
+    batch_free(b);
+    delete b;
+    return STATER_OK;
+}
