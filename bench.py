@@ -596,7 +596,7 @@ def serving_trace(njobs, seed=0):
     return jobs
 
 
-def run_serving_trace(S, jobs, rate, slots, precision, with_output=True, seed=1, chunk=32):
+def run_serving_trace(S, jobs, rate, slots, precision, with_output=True, seed=1, chunk=32, fuse=False):
     """Submits `jobs` at Poisson arrival times (rate jobs/s; rate <= 0: all at once)
     and returns the server statistics."""
     import numpy as np
@@ -605,7 +605,7 @@ def run_serving_trace(S, jobs, rate, slots, precision, with_output=True, seed=1,
     gaps = rng.exponential(1.0 / rate, len(jobs)) if rate > 0 else np.zeros(len(jobs))
     arrivals = np.cumsum(gaps)
     outs = [np.zeros((3, j["height"], j["width"]), np.float32) if with_output else None for j in jobs]
-    with serving.Server(max_slots=slots, precision=precision, chunk_spp=chunk) as srv:
+    with serving.Server(max_slots=slots, precision=precision, chunk_spp=chunk, fuse_small_jobs=fuse) as srv:
         t0 = time.perf_counter()
         for j, o, at in zip(jobs, outs, arrivals):
             delay = at - (time.perf_counter() - t0)
@@ -769,13 +769,23 @@ def measure_batch(S, njobs=32, steps=5, seed=11):
 def measure_serving(S, njobs, rate, slots, chunk, seed=0):
     """One Poisson arrival rate of the mixed-job trace through the serving engine."""
     jobs = serving_trace(njobs, seed=seed)
-    run_serving_trace(S, serving_trace(4, seed=99)[:4], 0, slots, S.F32)  # warm-up: scratch, tables
+    for fuse in (False, True):  # warm-up: scratch, tables, tuned tile heights
+        run_serving_trace(S, serving_trace(6, seed=99), 0, slots, S.F32, fuse=fuse)
+    res = {}
     with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
-        st = run_serving_trace(S, jobs, rate, slots, S.F32, chunk=chunk)
+        for fuse in (True, False):
+            res[fuse] = run_serving_trace(S, jobs, rate, slots, S.F32, chunk=chunk, fuse=fuse)
+    st = res[True]
+    small = sum(1 for j in jobs if j["width"] * j["height"] <= 512 * 512)
     return {"value": st["mpix_per_s"], "unit": UNIT, "rate_jobs_per_s": rate, "jobs": njobs, "slots": slots,
             "latency_ms": {"p50": st["latency_p50_ms"], "p99": st["latency_p99_ms"], "mean": st["latency_mean_ms"]},
             "completed": st["completed"], "failed": st["failed"], "peak_footprint_gb": st["peak_footprint_bytes"] / 1e9,
-            "workload": f"{njobs} jobs, resolutions {SERVE_RES}, spp {SERVE_SPP}, K {SERVE_K}, Poisson arrivals",
+            "fused_small_jobs": True, "small_jobs": small,
+            "without_fusion": {"value": res[False]["mpix_per_s"],
+                               "latency_ms": {"p50": res[False]["latency_p50_ms"], "p99": res[False]["latency_p99_ms"],
+                                              "mean": res[False]["latency_mean_ms"]}},
+            "workload": f"{njobs} jobs, resolutions {SERVE_RES}, spp {SERVE_SPP}, K {SERVE_K}, Poisson arrivals; "
+                        "small single-round jobs waiting together are fused into groups",
             "clocks": clk.summary()}
 
 

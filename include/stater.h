@@ -529,6 +529,11 @@ typedef struct {
     double hbm_budget_bytes;    /* admission limit; <= 0: 80% of the free memory at creation */
     int32_t precision;          /* STATER_F32 (serving form) or STATER_F64 (plain form) */
     int32_t chunk_spp;          /* samples generated and accumulated per step (default 32) */
+    /* 1: small single-round FP32 jobs (up to 512x512 pixels, 5 transforms) that
+     * wait together are admitted as one group onto one slot, and their denoise
+     * stages run as one launch per stage for the group (stater_batch); each
+     * job's output is bitwise the same as when it runs alone. */
+    int32_t fuse_small_jobs;
 } stater_server_config;
 
 typedef struct {

@@ -183,7 +183,7 @@ __device__ __forceinline__ void load_feat_scaled(float *dst, const float *__rest
     for (int idx = threadIdx.x; idx < A; idx += blockDim.x) {
         const int hy = idx / hw, hx = idx - hy * hw;
         const int gx = x0 - R + hx, gy = y0 - R + hy;
-        dst[idx] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? __ldg(src + (size_t)gy * W + gx) * mul : 0.f;
+        dst[idx] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? __fmul_rn(__ldg(src + (size_t)gy * W + gx), mul) : 0.f;
     }
 }
 
@@ -193,7 +193,7 @@ __device__ __forceinline__ void load_halo_scaled(float *dst, const float *__rest
     for (int idx = threadIdx.x; idx < A; idx += blockDim.x) {
         const int hy = idx / hw, hx = idx - hy * hw;
         const int gx = x0 - R + hx, gy = y0 - R + hy;
-        dst[idx] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? __ldg(src + (size_t)gy * W + gx) * mul : 0.f;
+        dst[idx] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? __fmul_rn(__ldg(src + (size_t)gy * W + gx), mul) : 0.f;
     }
 }
 
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P)
             for (int q = 0; q < kRows; q++) {
                 const int dy = r - q;
                 use[q] = vi[q] && dy >= -R && dy <= R;
-                spq[q] = P.ds2 * (float)(dy * dy);
+                spq[q] = __fmul_rn(P.ds2, (float)(dy * dy));
             }
 #pragma unroll 4
             for (int dx = -R; dx <= R; dx++) {
@@ -305,12 +305,12 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P)
 #pragma unroll
                 for (int q = 0; q < kRows; q++) {
                     if (!use[q]) continue;
-                    const float w = fast_exp2(range_arg2<MF>(fi[q], feat, A, h, nf, spq[q] + dxs));
-                    const float zz = zi[q][0] + zj[0];
+                    const float w = fast_exp2(range_arg2<MF>(fi[q], feat, A, h, nf, __fadd_rn(spq[q], dxs)));
+                    const float zz = __fadd_rn(zi[q][0], zj[0]);
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         const float dl = li[q][c] - lj[c];
-                        const float t = fmaf(-dl, dl, ZPIX ? zz : zi[q][c] + zj[c]);
+                        const float t = fmaf(-dl, dl, ZPIX ? zz : __fadd_rn(zi[q][c], zj[c]));
                         const float m = t >= 0.f ? w : 0.f;
                         aw[q][c] += m;
                         av[q][c] = fmaf(m, vj[c], av[q][c]);
@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) film_filter_f32(FastFilm P)
         float sw = 0.f, sf[3] = {0.f, 0.f, 0.f};
         for (int dy = -R; dy <= R; dy++) {
             const int row = (tr * kRows + q + R + dy) * hw + lx + R;
-            const float sdy = P.ds2 * (float)(dy * dy);
+            const float sdy = __fmul_rn(P.ds2, (float)(dy * dy));
             const uint64_t m = load_row(q, dy + R);
 #pragma unroll 4
             for (int dx = -R; dx <= R; dx++) {
@@ -647,7 +647,7 @@ __device__ __forceinline__ void ring_feat_fields(const FeatSet &fs, bool inb, si
                                                  float4 &b) {
     float v[8];
 #pragma unroll
-    for (int f = 0; f < kRingMF; f++) v[f] = (inb && f < fs.nch) ? __ldg(fs.plane[f] + g) * fs.mul[f] : 0.f;
+    for (int f = 0; f < kRingMF; f++) v[f] = (inb && f < fs.nch) ? __fmul_rn(__ldg(fs.plane[f] + g), fs.mul[f]) : 0.f;
     v[7] = last;
     a = f4(v[0], v[1], v[2], v[3]);
     b = f4(v[4], v[5], v[6], v[7]);
@@ -681,9 +681,9 @@ __device__ __forceinline__ float4 vars_ring_value(const FastVars &P, int rec, in
         v.y = zero ? 0.f : __ldg(src + HW + g);
         v.z = zero ? 0.f : __ldg(src + 2 * HW + g);
         if (ZPIX)
-            v.w = sub == 0 ? __ldg(P.se2[0] + g) * P.z2 : 0.f;
+            v.w = sub == 0 ? __fmul_rn(__ldg(P.se2[0] + g), P.z2) : 0.f;
         else
-            v.w = __ldg(P.se2[k] + (size_t)sub * HW + g) * P.z2;
+            v.w = __fmul_rn(__ldg(P.se2[k] + (size_t)sub * HW + g), P.z2);
     }
     return v;
 }
@@ -746,16 +746,16 @@ __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by
     const bool vi = in && __ldg(P.n + gi) >= 2;
     float fi[kRingMF];
 #pragma unroll
-    for (int f = 0; f < kRingMF; f++) fi[f] = (in && f < nf) ? __ldg(P.feat.plane[f] + gi) * P.feat.mul[f] : 0.f;
+    for (int f = 0; f < kRingMF; f++) fi[f] = (in && f < nf) ? __fmul_rn(__ldg(P.feat.plane[f] + gi), P.feat.mul[f]) : 0.f;
     float li[KMAX][3], zi[KMAX][3], aw[KMAX][3], av[KMAX][3], avc[KMAX][3];
-    const float zp = (ZPIX && in) ? __ldg(P.se2[0] + gi) * P.z2 : 0.f;
+    const float zp = (ZPIX && in) ? __fmul_rn(__ldg(P.se2[0] + gi), P.z2) : 0.f;
 #pragma unroll
     for (int k = 0; k < KMAX; k++)
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             const bool ok = in && k < K;
             li[k][c] = ok ? __ldg(P.lnS2[k] + (size_t)c * HW + gi) : 0.f;
-            zi[k][c] = ZPIX ? zp : (ok ? __ldg(P.se2[k] + (size_t)c * HW + gi) * P.z2 : 0.f);
+            zi[k][c] = ZPIX ? zp : (ok ? __fmul_rn(__ldg(P.se2[k] + (size_t)c * HW + gi), P.z2) : 0.f);
             aw[k][c] = av[k][c] = avc[k][c] = 0.f;
         }
     __syncthreads();
@@ -765,13 +765,13 @@ __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by
         if (next < hh) ring_load_now(ring, next % NS, next, hw, nrec, value);
         if (vi) {
             const float4 *rp = ring + (size_t)((tr + R + r) % NS) * nrec * hw + lx + R;
-            const float spq = P.ds2 * (float)(r * r);
+            const float spq = __fmul_rn(P.ds2, (float)(r * r));
 #pragma unroll 2
             for (int dx = -R; dx <= R; dx++) {
                 const float4 F0 = rp[dx], F1 = rp[hw + dx];
                 const float fj[kRingMF] = {F0.x, F0.y, F0.z, F0.w, F1.x, F1.y, F1.z};
                 const float dxs = fmaf(P.ds2, (float)(dx * dx), F1.w);
-                float e = spq + dxs;
+                float e = __fadd_rn(spq, dxs);
 #pragma unroll
                 for (int f = 0; f < kRingMF; f++) {
                     if (f < nf) {
@@ -788,11 +788,11 @@ __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by
                     const float4 T2 = TW == 3 ? tp[2 * hw] : f4(0.f, 0.f, 0.f, 0.f);
                     const float lj[3] = {T0.x, T0.y, T0.z}, vj[3] = {T1.x, T1.y, T1.z}, vcj[3] = {T2.x, T2.y, T2.z};
                     const float zj[3] = {T0.w, T1.w, T2.w};
-                    const float zz = zi[k][0] + T0.w;
+                    const float zz = __fadd_rn(zi[k][0], T0.w);
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         const float dl = li[k][c] - lj[c];
-                        const float t = fmaf(-dl, dl, ZPIX ? zz : zi[k][c] + zj[c]);
+                        const float t = fmaf(-dl, dl, ZPIX ? zz : __fadd_rn(zi[k][c], zj[c]));
                         const float m = t >= 0.f ? w : 0.f;
                         aw[k][c] += m;
                         av[k][c] = fmaf(m, vj[c], av[k][c]);
@@ -925,7 +925,7 @@ __device__ __forceinline__ void film_ring_body(const FastFilm &P, int bx, int by
     }
     float fi[kRingMF];
 #pragma unroll
-    for (int f = 0; f < kRingMF; f++) fi[f] = (in && f < nf) ? __ldg(P.feat.plane[f] + gi) * P.feat.mul[f] : 0.f;
+    for (int f = 0; f < kRingMF; f++) fi[f] = (in && f < nf) ? __fmul_rn(__ldg(P.feat.plane[f] + gi), P.feat.mul[f]) : 0.f;
     float mi[KMAX][3], di[KMAX][3];
 #pragma unroll
     for (int sl = 0; sl < KMAX; sl++)
@@ -1007,7 +1007,7 @@ __device__ __forceinline__ void film_ring_body(const FastFilm &P, int bx, int by
             }
             if (r == 0) cand |= 1ull << R;  // the centre is always kept
             // pass B: the lane's survivors, in increasing dx
-            const float sdy = P.ds2 * (float)(r * r);
+            const float sdy = __fmul_rn(P.ds2, (float)(r * r));
             while (cand) {
                 const int dx = __ffsll((long long)cand) - 1 - R;
                 cand &= cand - 1;
@@ -1563,7 +1563,7 @@ extern "C" stater_status stater_test_order(const stater_transform *transforms, i
 // ---------------------------------------------------------------------------
 // Batches: many small images through one launch per stage.
 //
-// A small image (256x256 is 2,048 ring tiles of 32x8) fills a fraction of the
+// A small image (256x256 is 256 ring tiles of 32x8) fills a fraction of the
 // GPU and pays a launch and a tail per stage. A batch runs the jobs' stages
 // together: every job's accumulation (with the film sums) and film image on
 // one stream, then each denoise stage as ONE launch covering the tiles of all
@@ -1573,7 +1573,9 @@ extern "C" stater_status stater_test_order(const stater_transform *transforms, i
 // single-image kernels, so each job's results are bitwise those of its
 // single-image calls. The first run of a batch tunes each class's tile height
 // on the real data and then records the whole sequence into a CUDA graph;
-// later runs replay the graph (one launch for the host).
+// later runs replay the graph (one launch for the host). The serving engine
+// uses the same tables for one-shot groups of small jobs, allocated and freed
+// in stream order (batch_denoise_once).
 // ---------------------------------------------------------------------------
 namespace stater {
 namespace {
@@ -1624,91 +1626,175 @@ __global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_batch(const FastF
     film_ring_body<KMAX, TY, JB>(P, local % tx, local / tx);
 }
 
-// Jobs of one ring instantiation.
+constexpr int kTys[3] = {4, 8, 16};
+int ty_index(int ty) { return ty == 4 ? 0 : ty == 8 ? 1 : 2; }
+
+// Jobs of one ring instantiation, with the tile offsets of every height.
 struct RingClass {
-    int filter;      // 0: variance filter, 1: film filter
+    int filter;  // 0: variance filter, 1: film filter
     int km, nrec, R;
     bool levc, zp, jb, feats;
     std::vector<int> jobs;
+    size_t pixels = 0;
     int ty = 0;
-    int ntiles = 0;
-    void *d_params = nullptr;  // the class's FastVars / FastFilm blocks
-    int *d_start = nullptr;
+    int ntiles[3] = {0, 0, 0};
+    size_t off_params = 0, off_start[3] = {0, 0, 0};  // into the device block
+    const void *d_params = nullptr;
+    const int *d_start[3] = {nullptr, nullptr, nullptr};
 };
 
-}  // namespace
-}  // namespace stater
-
-struct stater_batch {
-    int dev = 0;
-    int reset = 0;
-    std::vector<stater_batch_job> jobs;
-    std::vector<stater::FastVars> vars;
-    std::vector<stater::FastFilm> film;
-    std::vector<stater::RingClass> classes;
-    stater::FastVars *d_vars = nullptr;
-    stater::FastFilm *d_film = nullptr;
-    int *d_pix_start = nullptr;  // elementwise stages: blocks of 128 pixels per job
+// Host plan of a batch: parameter blocks, classes and one device block
+// holding every table (built once, uploaded with one copy).
+struct BatchPlan {
+    std::vector<FastVars> vars;
+    std::vector<FastFilm> film;
+    std::vector<RingClass> classes;
+    std::vector<unsigned char> host;  // the device block's contents
+    size_t off_vars = 0, off_film = 0, off_pix = 0, bytes = 0;
     int pix_blocks = 0, kmax = 1;
-    float *s2 = nullptr;         // per job s2 / s2c planes
-    bool recorded = false;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    cudaStream_t capture = nullptr;
-    bool ring_ok = true;
+    unsigned char *dev = nullptr;
+    FastVars *d_vars = nullptr;
+    FastFilm *d_film = nullptr;
+    const int *d_pix_start = nullptr;
 };
 
-namespace stater {
-namespace {
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-void batch_free(stater_batch *b) {
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->capture) cudaStreamDestroy(b->capture);
-    for (auto &c : b->classes) {
-        cudaFree(c.d_params);
-        cudaFree(c.d_start);
+// Validates the jobs and lays out the plan; s2 scratch (2 x 3 x K x HW floats
+// per job) starts at s2base. Device pointers are filled by plan_bind.
+stater_status plan_build(const stater_batch_job *jobs, int n, float *s2base, BatchPlan &B, bool need_acc) {
+    std::vector<int> pix_start;
+    B.vars.resize(n);
+    B.film.resize(n);
+    size_t off = 0;
+    int blocks = 0;
+    for (int j = 0; j < n; j++) {
+        const stater_batch_job &J = jobs[j];
+        const stater_accumulate_args &A = J.acc;
+        if ((need_acc && (A.precision != STATER_F32 || A.mode != STATER_ACC_FAST || !A.film_contrib_sum ||
+                          A.pixel_index)) ||
+            J.vars.precision != STATER_F32 || J.film.precision != STATER_F32 || !J.film_rgb)
+            return set_error(STATER_ERR_INVALID, "stater_batch_create: a batch runs the FP32 form with film sums, "
+                                                 "film_rgb and no pixel index");
+        if (J.vars.width != A.width || J.vars.height != A.height || J.film.width != A.width ||
+            J.film.height != A.height || J.vars.n_buffers != A.n_transforms || J.film.n_buffers != A.n_transforms ||
+            J.film.accept_bits)
+            return set_error(STATER_ERR_INVALID, "stater_batch_create: the stages of a job disagree");
+        stater_status st = fill_fast_vars(&J.vars, B.vars[j]);
+        if (st != STATER_OK) return st;
+        st = fill_fast_film(&J.film, B.film[j], nullptr);
+        if (st != STATER_OK) return st;
+        FastVars &V = B.vars[j];
+        const size_t HW = (size_t)V.W * V.H;
+        V.s2 = s2base + off;
+        V.s2c = V.s2 + (size_t)3 * V.K * HW;
+        off += (size_t)2 * 3 * V.K * HW;
+        pix_start.push_back(blocks);
+        blocks += (int)((HW + 127) / 128);
+        B.kmax = std::max(B.kmax, V.K);
+        const bool zp = V.max_moment < 4;
+        const int kmv = ring_kmax(V.K), nrv = kRingFW + V.K * ((V.levc || !zp) ? 3 : 2);
+        const FastFilm &F = B.film[j];
+        const int nrf = kRingFW + 1 + 2 * F.K;
+        if (!(kmv > 0 && ring_ty(V.R, nrv) > 0 && V.feat.nch <= kRingMF && ring_ty(F.R, nrf) > 0 &&
+              F.feat.nch <= kRingMF))
+            return set_error(STATER_ERR_UNSUPPORTED, "stater_batch_create: a job needs more than 5 transforms, 7 "
+                                                     "feature channels or more than the ring's shared memory");
+        for (int f = 0; f < 2; f++) {
+            RingClass key;
+            key.filter = f;
+            key.km = kmv;
+            key.nrec = f == 0 ? nrv : nrf;
+            key.R = f == 0 ? V.R : F.R;
+            key.levc = f == 0 && V.levc;
+            key.zp = f == 0 && zp;
+            key.jb = f == 1 && F.mt_mode == STATER_MT_JB;
+            key.feats = (f == 0 ? V.feat.nch : F.feat.nch) > 0;
+            RingClass *found = nullptr;
+            for (auto &c : B.classes)
+                if (c.filter == key.filter && c.km == key.km && c.nrec == key.nrec && c.R == key.R &&
+                    c.levc == key.levc && c.zp == key.zp && c.jb == key.jb && c.feats == key.feats)
+                    found = &c;
+            if (!found) {
+                B.classes.push_back(key);
+                found = &B.classes.back();
+            }
+            found->jobs.push_back(j);
+            found->pixels += HW;
+        }
     }
-    cudaFree(b->d_vars);
-    cudaFree(b->d_film);
-    cudaFree(b->d_pix_start);
-    cudaFree(b->s2);
+    pix_start.push_back(blocks);
+    B.pix_blocks = blocks;
+    // device block: job tables, pixel offsets, per class parameter blocks and tile offsets
+    size_t o = 0;
+    auto take = [&](size_t b) {
+        o = align_up(o, 256);
+        const size_t r = o;
+        o += b;
+        return r;
+    };
+    B.off_vars = take(sizeof(FastVars) * n);
+    B.off_film = take(sizeof(FastFilm) * n);
+    B.off_pix = take(sizeof(int) * pix_start.size());
+    std::vector<std::vector<int>> starts;
+    for (auto &c : B.classes) {
+        const size_t sz = c.filter == 0 ? sizeof(FastVars) : sizeof(FastFilm);
+        c.off_params = take(sz * c.jobs.size());
+        for (int t = 0; t < 3; t++) {
+            std::vector<int> st;
+            int total = 0;
+            for (int j : c.jobs) {
+                st.push_back(total);
+                const int W = c.filter == 0 ? B.vars[j].W : B.film[j].W, H = c.filter == 0 ? B.vars[j].H : B.film[j].H;
+                total += ((W + kTX2 - 1) / kTX2) * ((H + kTys[t] - 1) / kTys[t]);
+            }
+            st.push_back(total);
+            c.ntiles[t] = total;
+            c.off_start[t] = take(sizeof(int) * st.size());
+            starts.push_back(st);
+        }
+    }
+    B.bytes = align_up(o, 256);
+    B.host.assign(B.bytes, 0);
+    std::memcpy(B.host.data() + B.off_vars, B.vars.data(), sizeof(FastVars) * n);
+    std::memcpy(B.host.data() + B.off_film, B.film.data(), sizeof(FastFilm) * n);
+    std::memcpy(B.host.data() + B.off_pix, pix_start.data(), sizeof(int) * pix_start.size());
+    size_t si = 0;
+    for (auto &c : B.classes) {
+        const size_t sz = c.filter == 0 ? sizeof(FastVars) : sizeof(FastFilm);
+        for (size_t i = 0; i < c.jobs.size(); i++)
+            std::memcpy(B.host.data() + c.off_params + i * sz,
+                        c.filter == 0 ? (const void *)&B.vars[c.jobs[i]] : (const void *)&B.film[c.jobs[i]], sz);
+        for (int t = 0; t < 3; t++, si++)
+            std::memcpy(B.host.data() + c.off_start[t], starts[si].data(), sizeof(int) * starts[si].size());
+    }
+    return STATER_OK;
 }
 
-template <typename T>
-cudaError_t upload(T **dst, const T *src, size_t n) {
-    cudaError_t e = cudaMalloc(dst, sizeof(T) * (n ? n : 1));
-    if (e != cudaSuccess) return e;
-    return cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice);
+void plan_bind(BatchPlan &B, unsigned char *dev) {
+    B.dev = dev;
+    B.d_vars = (FastVars *)(dev + B.off_vars);
+    B.d_film = (FastFilm *)(dev + B.off_film);
+    B.d_pix_start = (const int *)(dev + B.off_pix);
+    for (auto &c : B.classes) {
+        c.d_params = dev + c.off_params;
+        for (int t = 0; t < 3; t++) c.d_start[t] = (const int *)(dev + c.off_start[t]);
+    }
 }
 
-cudaError_t launch_ring_class(stater_batch *b, RingClass &c, int ty, cudaStream_t s) {
-    // per-job ring tile offsets at this height
-    std::vector<int> start;
-    int total = 0;
-    for (int j : c.jobs) {
-        start.push_back(total);
-        const int W = c.filter == 0 ? b->vars[j].W : b->film[j].W, H = c.filter == 0 ? b->vars[j].H : b->film[j].H;
-        total += ((W + kTX2 - 1) / kTX2) * ((H + ty - 1) / ty);
-    }
-    start.push_back(total);
-    if (c.ty != ty || !c.d_start) {
-        cudaFree(c.d_start);
-        c.d_start = nullptr;
-        cudaError_t e = upload(&c.d_start, start.data(), start.size());
-        if (e != cudaSuccess) return e;
-        c.ty = ty;
-        c.ntiles = total;
-    }
+cudaError_t launch_ring_class(const RingClass &c, int ty, cudaStream_t s) {
+    const int t = ty_index(ty);
+    const int total = c.ntiles[t];
+    const int *start = c.d_start[t];
     const size_t sm = ring_smem(c.R, c.nrec, ty);
     const int nj = (int)c.jobs.size();
     cudaError_t e = cudaErrorInvalidValue;
     if (c.filter == 0) {
         const FastVars *P = (const FastVars *)c.d_params;
-#define STATER_BATCH_VARS(LV, ZV, KV, TV)                                                                  \
-    if (c.levc == LV && c.zp == ZV && c.km == KV && ty == TV) {                                              \
-        e = set_smem(vars_ring_batch<LV, ZV, KV, TV>, sm);                                                   \
-        if (e == cudaSuccess) vars_ring_batch<LV, ZV, KV, TV><<<total, kTX2 * TV, sm, s>>>(P, c.d_start, nj); \
+#define STATER_BATCH_VARS(LV, ZV, KV, TV)                                                                \
+    if (c.levc == LV && c.zp == ZV && c.km == KV && ty == TV) {                                            \
+        e = set_smem(vars_ring_batch<LV, ZV, KV, TV>, sm);                                                 \
+        if (e == cudaSuccess) vars_ring_batch<LV, ZV, KV, TV><<<total, kTX2 * TV, sm, s>>>(P, start, nj); \
     }
 #define STATER_BATCH_VARS_K(LV, ZV, TV) \
     STATER_BATCH_VARS(LV, ZV, 1, TV) STATER_BATCH_VARS(LV, ZV, 3, TV) STATER_BATCH_VARS(LV, ZV, 5, TV)
@@ -1723,10 +1809,10 @@ cudaError_t launch_ring_class(stater_batch *b, RingClass &c, int ty, cudaStream_
 #undef STATER_BATCH_VARS
     } else {
         const FastFilm *P = (const FastFilm *)c.d_params;
-#define STATER_BATCH_FILM(KV, TV, JV)                                                               \
-    if (c.km == KV && ty == TV && c.jb == JV) {                                                      \
-        e = set_smem(film_ring_batch<KV, TV, JV>, sm);                                               \
-        if (e == cudaSuccess) film_ring_batch<KV, TV, JV><<<total, kTX2 * TV, sm, s>>>(P, c.d_start, nj); \
+#define STATER_BATCH_FILM(KV, TV, JV)                                                             \
+    if (c.km == KV && ty == TV && c.jb == JV) {                                                    \
+        e = set_smem(film_ring_batch<KV, TV, JV>, sm);                                             \
+        if (e == cudaSuccess) film_ring_batch<KV, TV, JV><<<total, kTX2 * TV, sm, s>>>(P, start, nj); \
     }
 #define STATER_BATCH_FILM_T(TV, JV) STATER_BATCH_FILM(1, TV, JV) STATER_BATCH_FILM(3, TV, JV) STATER_BATCH_FILM(5, TV, JV)
         STATER_BATCH_FILM_T(16, false) STATER_BATCH_FILM_T(8, false) STATER_BATCH_FILM_T(4, false)
@@ -1737,7 +1823,64 @@ cudaError_t launch_ring_class(stater_batch *b, RingClass &c, int ty, cudaStream_
     return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
-// Enqueues one run of the batch on s. tune: pick the classes' tile heights first.
+// The batched denoise stages: variance statistics, variance filter, Welch
+// discriminators, film filter. tune: let the classes' tile heights be tuned.
+stater_status plan_enqueue_denoise(BatchPlan &B, int n, cudaStream_t s, bool tune) {
+    {
+        dim3 g((unsigned)B.pix_blocks, (unsigned)B.kmax);
+        vars_stats_batch<<<g, 128, 0, s>>>(B.d_vars, B.d_pix_start, n);
+        STATER_CHECK_LAUNCH("vars_stats_batch");
+    }
+    for (int pass = 0; pass < 2; pass++) {
+        if (pass == 1) {
+            dim3 g((unsigned)B.pix_blocks, (unsigned)B.kmax);
+            film_discr_batch<<<g, 128, 0, s>>>(B.d_film, B.d_pix_start, n);
+            STATER_CHECK_LAUNCH("film_discr_batch");
+        }
+        for (auto &c : B.classes) {
+            if (c.filter != pass) continue;
+            int ty = c.ty;
+            if (tune || !ty) {
+                const int variant = 64 + (c.filter == 0 ? (c.levc ? 1 : 0) + (c.zp ? 2 : 0) : (c.jb ? 1 : 0)) +
+                                    (c.feats ? 4 : 0);
+                ty = pick_ring_ty(c.filter, c.km, c.nrec, c.R, variant, c.pixels, s,
+                                  [&](int t) { return launch_ring_class(c, t, s); });
+                c.ty = ty;
+            }
+            cudaError_t e = launch_ring_class(c, ty, s);
+            if (e != cudaSuccess) return cuda_status(e, "batched ring filter");
+        }
+    }
+    return STATER_OK;
+}
+
+}  // namespace
+}  // namespace stater
+
+struct stater_batch {
+    int dev = 0;
+    int reset = 0;
+    std::vector<stater_batch_job> jobs;
+    stater::BatchPlan plan;
+    unsigned char *dev_block = nullptr;
+    float *s2 = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t capture = nullptr;
+};
+
+namespace stater {
+namespace {
+
+void batch_free(stater_batch *b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->capture) cudaStreamDestroy(b->capture);
+    cudaFree(b->dev_block);
+    cudaFree(b->s2);
+}
+
+// Enqueues one run of the batch on s.
 stater_status batch_enqueue(stater_batch *b, cudaStream_t s, bool tune) {
     const int n = (int)b->jobs.size();
     for (int j = 0; j < n; j++) {
@@ -1758,36 +1901,53 @@ stater_status batch_enqueue(stater_batch *b, cudaStream_t s, bool tune) {
                                       J.acc.film_spill, J.film_scale, J.film_rgb, (stater_stream)s);
         if (st != STATER_OK) return st;
     }
-    {
-        dim3 g((unsigned)b->pix_blocks, (unsigned)b->kmax);
-        vars_stats_batch<<<g, 128, 0, s>>>(b->d_vars, b->d_pix_start, n);
-        STATER_CHECK_LAUNCH("vars_stats_batch");
-    }
-    for (int pass = 0; pass < 2; pass++) {
-        if (pass == 1) {
-            dim3 g((unsigned)b->pix_blocks, (unsigned)b->kmax);
-            film_discr_batch<<<g, 128, 0, s>>>(b->d_film, b->d_pix_start, n);
-            STATER_CHECK_LAUNCH("film_discr_batch");
-        }
-        for (auto &c : b->classes) {
-            if (c.filter != pass) continue;
-            int ty = c.ty;
-            if (tune || !ty) {
-                size_t px = 0;
-                for (int j : c.jobs) px += (size_t)b->jobs[j].acc.width * b->jobs[j].acc.height;
-                const int variant = 64 + (c.filter == 0 ? (c.levc ? 1 : 0) + (c.zp ? 2 : 0) : (c.jb ? 1 : 0)) +
-                                    (c.feats ? 4 : 0);
-                ty = pick_ring_ty(c.filter, c.km, c.nrec, c.R, variant, px, s,
-                                  [&](int t) { return launch_ring_class(b, c, t, s); });
-            }
-            cudaError_t e = launch_ring_class(b, c, ty, s);
-            if (e != cudaSuccess) return cuda_status(e, "batched ring filter");
-        }
-    }
-    return STATER_OK;
+    return plan_enqueue_denoise(b->plan, n, s, tune);
+}
+
+size_t s2_floats(const stater_batch_job *jobs, int n) {
+    size_t f = 0;
+    for (int j = 0; j < n; j++)
+        f += (size_t)2 * 3 * std::max(jobs[j].acc.n_transforms, 1) * jobs[j].acc.width * jobs[j].acc.height;
+    return f;
 }
 
 }  // namespace
+
+// Serving engine: the batched denoise stages of a group of small jobs whose
+// samples are already accumulated and whose film images are made, enqueued on
+// s once (no graph). Tables and scratch are allocated and freed in stream
+// order; `staging` (pinned host memory of staging_bytes) carries the tables
+// and must stay untouched until the stream has passed this point.
+stater_status batch_denoise_once(const stater_batch_job *jobs, int n, cudaStream_t s, void *staging,
+                                 size_t staging_bytes) {
+    BatchPlan B;
+    const size_t s2b = align_up(sizeof(float) * s2_floats(jobs, n), 256);
+    stater_status st = plan_build(jobs, n, nullptr, B, false);
+    if (st != STATER_OK) return st;
+    if (B.bytes > staging_bytes)
+        return set_error(STATER_ERR_UNSUPPORTED, "batch_denoise_once: tables exceed the staging buffer");
+    unsigned char *dev = nullptr;
+    cudaError_t e = cudaMallocAsync((void **)&dev, B.bytes + s2b, s);
+    if (e != cudaSuccess) return cuda_status(e, "batch_denoise_once: tables");
+    // rebuild with the scratch placed after the tables
+    BatchPlan B2;
+    st = plan_build(jobs, n, (float *)(dev + B.bytes), B2, false);
+    if (st != STATER_OK) {
+        cudaFreeAsync(dev, s);
+        return st;
+    }
+    std::memcpy(staging, B2.host.data(), B2.bytes);
+    e = cudaMemcpyAsync(dev, staging, B2.bytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(dev, s);
+        return cuda_status(e, "batch_denoise_once: table upload");
+    }
+    plan_bind(B2, dev);
+    st = plan_enqueue_denoise(B2, n, s, !stream_capturing(s));
+    cudaFreeAsync(dev, s);
+    return st;
+}
+
 }  // namespace stater
 
 using namespace stater;
@@ -1807,91 +1967,14 @@ extern "C" stater_status stater_batch_create(const stater_batch_job *jobs, int32
         delete b;
         return st;
     };
-    size_t s2_floats = 0;
-    std::vector<int> pix_start;
-    for (int j = 0; j < n_jobs; j++) {
-        const stater_batch_job &J = jobs[j];
-        const stater_accumulate_args &A = J.acc;
-        if (A.precision != STATER_F32 || A.mode != STATER_ACC_FAST || J.vars.precision != STATER_F32 ||
-            J.film.precision != STATER_F32)
-            return fail(set_error(STATER_ERR_INVALID, "stater_batch_create: a batch runs the FP32 form only"));
-        if (!A.film_contrib_sum || !J.film_rgb || A.pixel_index)
-            return fail(set_error(STATER_ERR_INVALID, "stater_batch_create: jobs need film sums, film_rgb and no "
-                                                      "pixel index"));
-        if (J.vars.width != A.width || J.vars.height != A.height || J.film.width != A.width ||
-            J.film.height != A.height || J.vars.n_buffers != A.n_transforms || J.film.n_buffers != A.n_transforms ||
-            J.film.accept_bits)
-            return fail(set_error(STATER_ERR_INVALID, "stater_batch_create: the stages of a job disagree"));
-        s2_floats += (size_t)2 * 3 * A.n_transforms * A.width * A.height;
-    }
-    cudaError_t ce = cudaMalloc(&b->s2, sizeof(float) * (s2_floats ? s2_floats : 1));
+    cudaError_t ce = cudaMalloc(&b->s2, sizeof(float) * std::max<size_t>(s2_floats(jobs, n_jobs), 1));
     if (ce != cudaSuccess) return fail(cuda_status(ce, "stater_batch_create: scratch"));
-    b->vars.resize(n_jobs);
-    b->film.resize(n_jobs);
-    size_t off = 0;
-    int blocks = 0;
-    for (int j = 0; j < n_jobs; j++) {
-        const stater_batch_job &J = jobs[j];
-        stater_status st = fill_fast_vars(&J.vars, b->vars[j]);
-        if (st != STATER_OK) return fail(st);
-        st = fill_fast_film(&J.film, b->film[j], nullptr);
-        if (st != STATER_OK) return fail(st);
-        FastVars &V = b->vars[j];
-        const size_t HW = (size_t)V.W * V.H;
-        V.s2 = b->s2 + off;
-        V.s2c = V.s2 + (size_t)3 * V.K * HW;
-        off += (size_t)2 * 3 * V.K * HW;
-        pix_start.push_back(blocks);
-        blocks += (int)((HW + 127) / 128);
-        b->kmax = std::max(b->kmax, V.K);
-        // ring classes (jobs outside the ring kernels' range are not batched)
-        const bool zp = V.max_moment < 4;
-        const int kmv = ring_kmax(V.K), nrv = kRingFW + V.K * ((V.levc || !zp) ? 3 : 2);
-        const FastFilm &F = b->film[j];
-        const int nrf = kRingFW + 1 + 2 * F.K;
-        if (!(kmv > 0 && ring_ty(V.R, nrv) > 0 && V.feat.nch <= kRingMF && ring_ty(F.R, nrf) > 0 &&
-              F.feat.nch <= kRingMF))
-            return fail(set_error(STATER_ERR_UNSUPPORTED, "stater_batch_create: a job needs more than 5 transforms, "
-                                                          "7 feature channels or the ring's shared memory"));
-        for (int f = 0; f < 2; f++) {
-            RingClass key;
-            key.filter = f;
-            key.km = kmv;
-            key.nrec = f == 0 ? nrv : nrf;
-            key.R = f == 0 ? V.R : F.R;
-            key.levc = f == 0 && V.levc;
-            key.zp = f == 0 && zp;
-            key.jb = f == 1 && F.mt_mode == STATER_MT_JB;
-            key.feats = (f == 0 ? V.feat.nch : F.feat.nch) > 0;
-            RingClass *found = nullptr;
-            for (auto &c : b->classes)
-                if (c.filter == key.filter && c.km == key.km && c.nrec == key.nrec && c.R == key.R &&
-                    c.levc == key.levc && c.zp == key.zp && c.jb == key.jb && c.feats == key.feats)
-                    found = &c;
-            if (!found) {
-                b->classes.push_back(key);
-                found = &b->classes.back();
-            }
-            found->jobs.push_back(j);
-        }
-    }
-    pix_start.push_back(blocks);
-    b->pix_blocks = blocks;
-    if ((ce = upload(&b->d_vars, b->vars.data(), b->vars.size())) != cudaSuccess ||
-        (ce = upload(&b->d_film, b->film.data(), b->film.size())) != cudaSuccess ||
-        (ce = upload(&b->d_pix_start, pix_start.data(), pix_start.size())) != cudaSuccess)
+    stater_status st = plan_build(jobs, n_jobs, b->s2, b->plan, true);
+    if (st != STATER_OK) return fail(st);
+    if ((ce = cudaMalloc(&b->dev_block, b->plan.bytes)) != cudaSuccess ||
+        (ce = cudaMemcpy(b->dev_block, b->plan.host.data(), b->plan.bytes, cudaMemcpyHostToDevice)) != cudaSuccess)
         return fail(cuda_status(ce, "stater_batch_create: job tables"));
-    for (auto &c : b->classes) {
-        std::vector<unsigned char> blob;
-        const size_t sz = c.filter == 0 ? sizeof(FastVars) : sizeof(FastFilm);
-        blob.resize(sz * c.jobs.size());
-        for (size_t i = 0; i < c.jobs.size(); i++)
-            std::memcpy(blob.data() + i * sz,
-                        c.filter == 0 ? (const void *)&b->vars[c.jobs[i]] : (const void *)&b->film[c.jobs[i]], sz);
-        if ((ce = cudaMalloc(&c.d_params, blob.size())) != cudaSuccess ||
-            (ce = cudaMemcpy(c.d_params, blob.data(), blob.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-            return fail(cuda_status(ce, "stater_batch_create: class tables"));
-    }
+    plan_bind(b->plan, b->dev_block);
     *out = b;
     return STATER_OK;
 }

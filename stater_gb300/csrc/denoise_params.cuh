@@ -72,5 +72,9 @@ inline bool fill_gbuf(GBuf<T> &g, const stater_gbuffers &in) {
 // FP32 form entry points (denoise_fast.cu).
 stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s);
 stater_status denoise_film_f32(const stater_denoise_film_args *a, cudaStream_t s);
+// The batched denoise stages of jobs already accumulated, with their film
+// images made, enqueued once on s (serving engine; denoise_fast.cu).
+stater_status batch_denoise_once(const stater_batch_job *jobs, int n, cudaStream_t s, void *staging,
+                                 size_t staging_bytes);
 
 }  // namespace stater

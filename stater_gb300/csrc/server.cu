@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "denoise_params.cuh"
 
 namespace stater {
 namespace {
@@ -165,6 +166,7 @@ struct Job {
     double footprint = 0;
     unsigned char *base = nullptr;
     cudaEvent_t ev = nullptr;
+    std::shared_ptr<int> group_left;  // fused group: jobs of the group not finished yet
     Clock::time_point t_submit, t_done;
     double latency_ms = 0;
 };
@@ -173,8 +175,18 @@ struct Slot {
     cudaStream_t stream = nullptr;
     int32_t *hmax = nullptr;  // pinned: largest target of the last round
     int32_t *hact = nullptr;  // pinned: active prefix length of each step of the next round
+    void *staging = nullptr;  // pinned: job tables of a fused group
     bool busy = false;
 };
+
+// Small single-round jobs admitted together run as one group on one slot: each
+// job's samples are generated and accumulated on the slot's stream, then the
+// denoise stages of the whole group run as one launch per stage (the batched
+// kernels of stater_batch), so small images no longer pay a launch and a tail
+// per stage each. Results are bitwise those of the same job run alone.
+constexpr size_t kFuseMaxPixels = (size_t)512 * 512;
+constexpr int kFuseMaxJobs = 16;
+constexpr size_t kStagingBytes = (size_t)1 << 20;
 
 }  // namespace
 }  // namespace stater
@@ -202,6 +214,8 @@ struct stater_server {
 
     void run();
     bool start(Job &j);
+    bool start_group(std::vector<std::shared_ptr<Job>> &group);
+    bool fusable(const Job &j) const;
     bool enqueue_round(Job &j, int samples, bool uniform);
     bool enqueue_after_round(Job &j);
     void finish(Job &j, bool ok);
@@ -210,6 +224,12 @@ struct stater_server {
 namespace {
 
 stater_precision prec_of(const stater_server *s) { return (stater_precision)s->cfg.precision; }
+
+double group_footprint(const std::vector<std::shared_ptr<Job>> &g) {
+    double f = 0;
+    for (auto &j : g) f += j->footprint;
+    return f;
+}
 
 void fill_gbuffers(stater_gbuffers &g, const Job &j) {
     std::memset(&g, 0, sizeof(g));
@@ -299,11 +319,12 @@ bool stater_server::enqueue_round(Job &j, int samples, bool uniform) {
     return true;
 }
 
-// After a round: denoise the variance; then either allot the next round's
-// samples (and fetch their maximum) or filter the film and copy it out.
-bool stater_server::enqueue_after_round(Job &j) {
-    const Slot &sl = slots[j.slot];
-    cudaStream_t s = sl.stream;
+namespace {
+
+// The denoiseVars and denoiseFilm arguments of a job over its device block
+// (film = the FP32 film image; the FP64 form passes its widened copy).
+void job_denoise_args(const Job &j, stater_precision prec, stater_denoise_vars_args &v,
+                      stater_denoise_film_args &f) {
     const Layout &L = j.L;
     const size_t plane3 = 3 * L.HW * L.T;
     unsigned char *out6 = j.base + L.off_out6;
@@ -312,7 +333,7 @@ bool stater_server::enqueue_after_round(Job &j) {
     auto moment = [&](int k, int q) { return (void *)(stats + ((size_t)k * STATER_NQ + q) * plane3); };
     stater_gbuffers gb;
     fill_gbuffers(gb, j);
-    stater_denoise_vars_args v{};
+    std::memset(&v, 0, sizeof(v));
     v.n_buffers = j.d.n_transforms;
     v.width = j.d.width;
     v.height = j.d.height;
@@ -320,7 +341,7 @@ bool stater_server::enqueue_after_round(Job &j) {
     v.ds_factor = -0.5f / (j.d.filter_sd * j.d.filter_sd);
     v.var_z = j.d.var_z;
     v.max_moment = j.d.max_moment;
-    v.precision = prec_of(this);
+    v.precision = prec;
     v.n = (const int32_t *)(j.base + L.off_n);
     for (int k = 0; k < j.d.n_transforms; k++) {
         v.m2[k] = moment(k, STATER_Q_M2);
@@ -336,6 +357,46 @@ bool stater_server::enqueue_after_round(Job &j) {
         v.varCD[k] = out_of(4, k);
     }
     v.gbuffers = gb;
+    std::memset(&f, 0, sizeof(f));
+    f.n_buffers = j.d.n_transforms;
+    f.width = j.d.width;
+    f.height = j.d.height;
+    f.filter_radius = j.d.filter_radius;
+    f.ds_factor = v.ds_factor;
+    f.alpha = j.d.alpha;
+    f.mt_mode = STATER_MT_ALL;
+    f.use_levc = j.d.max_moment >= 5 ? 1 : 0;
+    f.precision = prec;
+    f.n = v.n;
+    f.film = L.T == 8 ? (const void *)(j.base + L.off_rgb64) : (const void *)(j.base + L.off_rgb);
+    for (int k = 0; k < j.d.n_transforms; k++) {
+        f.mean[k] = moment(k, STATER_Q_MEAN);
+        f.varD[k] = v.varD[k];
+        f.varCD[k] = v.varCD[k];
+        f.jb[k] = v.jb[k];
+        f.discr[k] = out_of(5, k);
+        f.m2[k] = v.m2[k];
+        f.m2C[k] = v.m2C[k];
+    }
+    f.gbuffers = gb;
+    f.filmD = j.base + L.off_filmD;
+    stater_test_order(j.d.transforms, j.d.n_transforms, f.test_order);
+}
+
+}  // namespace
+
+// After a round: denoise the variance; then either allot the next round's
+// samples (and fetch their maximum) or filter the film and copy it out.
+bool stater_server::enqueue_after_round(Job &j) {
+    const Slot &sl = slots[j.slot];
+    cudaStream_t s = sl.stream;
+    const Layout &L = j.L;
+    const size_t plane3 = 3 * L.HW * L.T;
+    unsigned char *stats = j.base + L.off_stats;
+    auto moment = [&](int k, int q) { return (void *)(stats + ((size_t)k * STATER_NQ + q) * plane3); };
+    stater_denoise_vars_args v;
+    stater_denoise_film_args f;
+    job_denoise_args(j, prec_of(this), v, f);
     if (stater_denoise_vars(&v, (stater_stream)s) != STATER_OK) return false;
     j.round++;
     if (j.round < j.d.rounds) {
@@ -365,35 +426,11 @@ bool stater_server::enqueue_after_round(Job &j) {
         if (stater_film_update_image(j.d.width, j.d.height, fs, fs + 3 * L.HW, fs + 4 * L.HW, 1.0f, rgb,
                                      (stater_stream)s) != STATER_OK)
             return false;
-        const void *film = rgb;
         if (L.T == 8) {
             widen_kernel<<<(unsigned)((3 * L.HW + 255) / 256), 256, 0, s>>>(3 * L.HW, rgb,
                                                                           (double *)(j.base + L.off_rgb64));
             if (cudaGetLastError() != cudaSuccess) return false;
-            film = j.base + L.off_rgb64;
         }
-        stater_denoise_film_args f{};
-        f.n_buffers = j.d.n_transforms;
-        f.width = j.d.width;
-        f.height = j.d.height;
-        f.filter_radius = j.d.filter_radius;
-        f.ds_factor = v.ds_factor;
-        f.alpha = j.d.alpha;
-        f.mt_mode = STATER_MT_ALL;
-        f.use_levc = j.d.max_moment >= 5 ? 1 : 0;
-        f.precision = prec_of(this);
-        f.n = v.n;
-        f.film = film;
-        for (int k = 0; k < j.d.n_transforms; k++) {
-            f.mean[k] = moment(k, STATER_Q_MEAN);
-            f.varD[k] = v.varD[k];
-            f.varCD[k] = v.varCD[k];
-            f.jb[k] = v.jb[k];
-            f.discr[k] = out_of(5, k);
-        }
-        f.gbuffers = gb;
-        f.filmD = j.base + L.off_filmD;
-        if (stater_test_order(j.d.transforms, j.d.n_transforms, f.test_order) != STATER_OK) return false;
         if (stater_denoise_film(&f, (stater_stream)s) != STATER_OK) return false;
         if (j.d.out_host) {
             if (L.T == 4) {
@@ -407,6 +444,53 @@ bool stater_server::enqueue_after_round(Job &j) {
         j.final_enqueued = true;
     }
     return cudaEventRecord(j.ev, s) == cudaSuccess;
+}
+
+bool stater_server::fusable(const Job &j) const {
+    return cfg.fuse_small_jobs && cfg.precision == STATER_F32 && j.d.rounds == 1 && j.L.HW <= kFuseMaxPixels &&
+           j.d.n_transforms <= 5 && j.d.n_features <= 7;
+}
+
+bool stater_server::start_group(std::vector<std::shared_ptr<Job>> &group) {
+    const int slot = group[0]->slot;
+    Slot &sl = slots[slot];
+    cudaStream_t s = sl.stream;
+    std::vector<stater_batch_job> bj(group.size());
+    for (size_t i = 0; i < group.size(); i++) {
+        Job &j = *group[i];
+        if (cudaMallocAsync((void **)&j.base, j.L.total, s) != cudaSuccess) {
+            cudaGetLastError();
+            j.base = nullptr;
+            return false;
+        }
+        if (cudaMemsetAsync(j.base, 0, j.L.off_samples, s) != cudaSuccess) return false;
+        if (cudaEventCreateWithFlags(&j.ev, cudaEventDisableTiming) != cudaSuccess) return false;
+        if (!enqueue_round(j, j.d.spp, true)) return false;
+        const float *fs = (const float *)(j.base + j.L.off_film);
+        float *rgb = (float *)(j.base + j.L.off_rgb);
+        if (stater_film_update_image(j.d.width, j.d.height, fs, fs + 3 * j.L.HW, fs + 4 * j.L.HW, 1.0f, rgb,
+                                     (stater_stream)s) != STATER_OK)
+            return false;
+        std::memset(&bj[i], 0, sizeof(bj[i]));
+        bj[i].acc.width = j.d.width;
+        bj[i].acc.height = j.d.height;
+        bj[i].acc.n_transforms = j.d.n_transforms;
+        bj[i].film_rgb = rgb;
+        bj[i].film_scale = 1.0f;
+        job_denoise_args(j, STATER_F32, bj[i].vars, bj[i].film);
+    }
+    if (batch_denoise_once(bj.data(), (int)bj.size(), s, sl.staging, kStagingBytes) != STATER_OK) return false;
+    for (auto &jp : group) {
+        Job &j = *jp;
+        if (j.d.out_host &&
+            cudaMemcpyAsync(j.d.out_host, j.base + j.L.off_filmD, 3 * j.L.HW * 4, cudaMemcpyDeviceToHost, s) !=
+                cudaSuccess)
+            return false;
+        j.round = 1;
+        j.final_enqueued = true;
+        if (cudaEventRecord(j.ev, s) != cudaSuccess) return false;
+    }
+    return true;
 }
 
 bool stater_server::start(Job &j) {
@@ -427,7 +511,8 @@ void stater_server::finish(Job &j, bool ok) {
         Slot &sl = slots[j.slot];
         if (j.base) cudaFreeAsync(j.base, sl.stream);
         if (!ok) cudaStreamSynchronize(sl.stream);
-        sl.busy = false;
+        // a fused group holds its slot until its last job is finished
+        if (!j.group_left || --*j.group_left == 0) sl.busy = false;
     }
     if (j.ev) cudaEventDestroy(j.ev);
     j.ev = nullptr;
@@ -457,6 +542,7 @@ void stater_server::run() {
     cudaSetDevice(device);
     while (true) {
         std::vector<std::shared_ptr<Job>> to_start;
+        std::vector<std::vector<std::shared_ptr<Job>>> groups;
         {
             std::unique_lock<std::mutex> lk(mu);
             if (stop && queue.empty() && active.empty()) break;
@@ -471,18 +557,41 @@ void stater_server::run() {
                 const bool fits = used + j->footprint <= budget || active.empty();
                 if (free_slot < 0 || !fits) break;
                 slots[free_slot].busy = true;
-                j->slot = free_slot;
-                j->state = STATER_JOB_RUNNING;
-                used += j->footprint;
+                // small single-round jobs waiting together share the slot as one group
+                std::vector<std::shared_ptr<Job>> group;
+                if (fusable(*j)) {
+                    group.push_back(j);
+                    queue.pop_front();
+                    while (!queue.empty() && (int)group.size() < kFuseMaxJobs && fusable(*queue.front()) &&
+                           used + group_footprint(group) + queue.front()->footprint <= budget) {
+                        group.push_back(queue.front());
+                        queue.pop_front();
+                    }
+                } else {
+                    group.push_back(j);
+                    queue.pop_front();
+                }
+                auto left = group.size() > 1 ? std::make_shared<int>((int)group.size()) : nullptr;
+                for (auto &g : group) {
+                    g->slot = free_slot;
+                    g->state = STATER_JOB_RUNNING;
+                    g->group_left = left;
+                    used += g->footprint;
+                    active.push_back(g);
+                }
                 peak = std::max(peak, used);
-                active.push_back(j);
-                to_start.push_back(j);
-                queue.pop_front();
+                if (group.size() > 1 || fusable(*group[0]))
+                    groups.push_back(group);
+                else
+                    to_start.push_back(group[0]);
             }
         }
         for (auto &j : to_start)
             if (!start(*j)) finish(*j, false);
-        bool progressed = !to_start.empty();
+        for (auto &g : groups)
+            if (!start_group(g))
+                for (auto &j : g) finish(*j, false);
+        bool progressed = !to_start.empty() || !groups.empty();
         std::vector<std::shared_ptr<Job>> snapshot;
         {
             std::lock_guard<std::mutex> lk(mu);
@@ -544,7 +653,8 @@ stater_status stater_server_create(const stater_server_config *cfg, stater_serve
     for (auto &sl : s->slots) {
         if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaMallocHost(&sl.hmax, sizeof(int32_t)) != cudaSuccess ||
-            cudaMallocHost(&sl.hact, sizeof(int32_t) * (kBins + 2)) != cudaSuccess) {
+            cudaMallocHost(&sl.hact, sizeof(int32_t) * (kBins + 2)) != cudaSuccess ||
+            cudaMallocHost(&sl.staging, kStagingBytes) != cudaSuccess) {
             cudaGetLastError();
             delete s;
             return set_error(STATER_ERR_CUDA, "stater_server_create: stream or pinned allocation failed");
@@ -671,6 +781,7 @@ stater_status stater_server_destroy(stater_server *srv) {
         }
         if (sl.hmax) cudaFreeHost(sl.hmax);
         if (sl.hact) cudaFreeHost(sl.hact);
+        if (sl.staging) cudaFreeHost(sl.staging);
     }
     delete srv;
     return STATER_OK;

@@ -12,7 +12,7 @@ from .api import transform_codes
 
 class ServerConfig(C.Structure):
     _fields_ = [("max_slots", C.c_int32), ("hbm_budget_bytes", C.c_double), ("precision", C.c_int32),
-                ("chunk_spp", C.c_int32)]
+                ("chunk_spp", C.c_int32), ("fuse_small_jobs", C.c_int32)]
 
 
 class JobDesc(C.Structure):
@@ -81,9 +81,9 @@ class Server:
     """Continuous-batching denoise server on the current CUDA device."""
 
     def __init__(self, max_slots: int = 4, hbm_budget_bytes: float = 0.0, precision: int = L.F32,
-                 chunk_spp: int = 32):
+                 chunk_spp: int = 32, fuse_small_jobs: bool = False):
         self.lib = _bind()
-        cfg = ServerConfig(max_slots, hbm_budget_bytes, precision, chunk_spp)
+        cfg = ServerConfig(max_slots, hbm_budget_bytes, precision, chunk_spp, int(bool(fuse_small_jobs)))
         h = C.c_void_p()
         L.call("stater_server_create", C.byref(cfg), C.byref(h))
         self.h = h

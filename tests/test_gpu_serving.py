@@ -124,3 +124,29 @@ def test_submit_rejects_bad_jobs(S):
             srv.submit(serving.job_desc(width=0, height=10, spp=4))
         with pytest.raises(StaterError):  # larger than the whole budget
             srv.submit(serving.job_desc(width=512, height=512, spp=4))
+
+
+def test_fused_small_jobs_equal_alone(S):
+    """Small single-round jobs that wait together run as one fused group (one
+    launch per denoise stage for the group); each job's film must equal the same
+    job run alone, and a larger or adaptive job in the mix is unaffected."""
+    from stater_gb300 import serving
+    small = [dict(width=128, height=96, spp=24, transforms=BASE_TR, radius=10, seed=11),
+             dict(width=256, height=256, spp=16, transforms=("identity", "log1p", "sqrt"), radius=10, seed=12),
+             dict(width=64, height=48, spp=32, transforms=("identity",), radius=6, seed=13),
+             dict(width=200, height=120, spp=20, transforms=("identity", ("boxcox", 0.25)), max_moment=5, radius=7,
+                  seed=14),
+             dict(width=512, height=512, spp=8, transforms=BASE_TR, radius=10, seed=15)]
+    other = [dict(width=640, height=360, spp=16, transforms=BASE_TR, radius=10, seed=16),
+             dict(width=96, height=80, spp=24, rounds=2, transforms=BASE_TR, radius=5, seed=17)]
+    alone = [_run_alone(serving, m) for m in small + other]
+    jobs = small + other
+    outs = [_out(m["width"], m["height"]) for m in jobs]
+    with serving.Server(max_slots=2, fuse_small_jobs=True) as srv:
+        for m, o in zip(jobs, outs):
+            srv.submit(serving.job_desc(**m, out=o), keepalive=o)
+        srv.drain()
+        st = srv.stats()
+    assert st["completed"] == len(jobs) and st["failed"] == 0
+    for i, (o, a) in enumerate(zip(outs, alone)):
+        assert np.array_equal(o, a), i
