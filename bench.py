@@ -478,7 +478,11 @@ def run_gpu(args, rank, world, dist):
         # from pinned host memory on this host link) while the accumulation of
         # the previous chunk runs; 16-spp chunks left gaps between the copies
         chunk = 32
-        host = torch.empty(SPP, 5 + G, H, W, dtype=torch.float32, pin_memory=True)
+        # page-locked host memory on huge pages (stater_host_alloc): with base
+        # pages, copies of this 25.5 GB buffer varied between 65 and 210 GB/s
+        # from run to run; on huge pages they hold the link's 210 GB/s
+        host_buf = S.HostBuffer((SPP, 5 + G, H, W))
+        host = host_buf.tensor
         first = torch.zeros(H, W, dtype=torch.int32, device="cuda")
         tmp = torch.empty(chunk, 5 + G, H, W, dtype=torch.float32, device="cuda")
         for c0 in range(0, SPP, chunk):
@@ -534,9 +538,10 @@ def run_gpu(args, rank, world, dist):
         e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 3 * HW * 4, "ms_per_step": e2e_ms,
                "h2d_gbs": h2d / (e2e_ms / 1e3) / 1e9, "link_gbs_copies_alone": link_gbs,
-               "path": "pinned host samples -> 32-spp chunks (copy stream) -> accumulate + film sums -> film image "
-                       "-> denoise -> filmD to host"}
+               "path": "page-locked huge-page host samples (stater_host_alloc) -> 32-spp chunks (copy stream) -> "
+                       "accumulate + film sums -> film image -> denoise -> filmD to host"}
         del host, stage
+        host_buf.close()
         torch.cuda.empty_cache()
 
     # the other configurations, compact: LEV at 1080p/512 spp, adaptive rounds,
@@ -766,6 +771,16 @@ def measure_batch(S, njobs=32, steps=5, seed=11):
     return out
 
 
+def small_trace(njobs, seed=0):
+    """Small single-round jobs only: 256x256 or 512x512, 16 or 64 spp, K 1/3/5."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    tr = WORKLOAD["transforms"]
+    return [dict(width=int(side), height=int(side), spp=int(rng.choice([16, 64])),
+                 transforms=tuple(tr[:int(rng.choice([1, 3, 5]))]), radius=WORKLOAD["radius"], seed=700 + i)
+            for i, side in enumerate(rng.choice([256, 512], size=njobs))]
+
+
 def measure_serving(S, njobs, rate, slots, chunk, seed=0):
     """One Poisson arrival rate of the mixed-job trace through the serving engine."""
     jobs = serving_trace(njobs, seed=seed)
@@ -775,12 +790,23 @@ def measure_serving(S, njobs, rate, slots, chunk, seed=0):
     with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
         for fuse in (True, False):
             res[fuse] = run_serving_trace(S, jobs, rate, slots, S.F32, chunk=chunk, fuse=fuse)
+        # a stream of small jobs only, where fusion has work to fuse
+        sjobs = small_trace(48, seed=seed)
+        for fuse in (True, False):
+            res[("small", fuse)] = run_serving_trace(S, sjobs, 2000.0, slots, S.F32, chunk=chunk, fuse=fuse)
     st = res[True]
     small = sum(1 for j in jobs if j["width"] * j["height"] <= 512 * 512)
+    small_only = {}
+    for fuse in (True, False):
+        r = res[("small", fuse)]
+        small_only["fused" if fuse else "not_fused"] = {
+            "value": r["mpix_per_s"], "latency_ms": {"p50": r["latency_p50_ms"], "p99": r["latency_p99_ms"]}}
     return {"value": st["mpix_per_s"], "unit": UNIT, "rate_jobs_per_s": rate, "jobs": njobs, "slots": slots,
             "latency_ms": {"p50": st["latency_p50_ms"], "p99": st["latency_p99_ms"], "mean": st["latency_mean_ms"]},
             "completed": st["completed"], "failed": st["failed"], "peak_footprint_gb": st["peak_footprint_bytes"] / 1e9,
             "fused_small_jobs": True, "small_jobs": small,
+            "small_jobs_only": dict(small_only, workload="48 jobs of 256x256 or 512x512, 16 or 64 spp, K 1/3/5, "
+                                                          "Poisson arrivals at 2000 jobs/s"),
             "without_fusion": {"value": res[False]["mpix_per_s"],
                                "latency_ms": {"p50": res[False]["latency_p50_ms"], "p99": res[False]["latency_p99_ms"],
                                               "mean": res[False]["latency_mean_ms"]}},

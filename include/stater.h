@@ -149,6 +149,16 @@ stater_status stater_debug_set_pipeline_waits(uint32_t wait_polls, int32_t stall
  * device float [blocks], written only if a chain reaches an impossible value. */
 stater_status stater_fp32_peak_probe(int32_t blocks, int32_t iters, int32_t packed, float *sink, double *flops,
                                      stater_stream stream);
+/* Page-locked host memory for sample buffers (no counterpart in the reference,
+ * whose Estimator pins its host buffers through OpenCV's allocator,
+ * estimator.h:382). The memory is mapped anonymously on huge pages where the
+ * operating system offers transparent huge pages, zeroed and registered with
+ * CUDA, so copies from it run at the host link's rate every time: with base
+ * pages, copies of tens of GB varied between about 65 and 210 GB/s from run to
+ * run on a GB300 host, and from huge pages held 210 GB/s. Free with
+ * stater_host_free and the same size. */
+stater_status stater_host_alloc(size_t bytes, void **out);
+stater_status stater_host_free(void *ptr, size_t bytes);
 /* Releases cached device scratch and tables of the current device and forgets
  * the cached device addresses of the library's fixed arrays. Call it before a
  * device reset (cudaDeviceReset) that is followed by further calls into the

@@ -125,6 +125,8 @@ def load() -> C.CDLL:
         "stater_last_error": (C.c_char_p, []),
         "stater_abi_version": (C.c_int32, []),
         "stater_release_cache": (st, []),
+        "stater_host_alloc": (st, [C.c_size_t, C.POINTER(VP)]),
+        "stater_host_free": (st, [VP, C.c_size_t]),
         "stater_debug_set_pipeline_waits": (st, [C.c_uint32, C.c_int32]),
         "stater_fp32_peak_probe": (st, [C.c_int32, C.c_int32, C.c_int32, VP, C.POINTER(C.c_double), VP]),
         "stater_accumulate": (st, [C.POINTER(AccumulateArgs), VP]),

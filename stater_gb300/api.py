@@ -389,6 +389,36 @@ class Batch:
             pass
 
 
+class HostBuffer:
+    """Page-locked host memory on huge pages (stater_host_alloc), viewed as a
+    float32 torch tensor of `shape` on the CPU: the source of host-to-device
+    sample copies that run at the link's rate every time."""
+
+    def __init__(self, shape, dtype=torch.float32):
+        import numpy as np
+        n = 1
+        for d in shape:
+            n *= int(d)
+        self.bytes = n * torch.empty(0, dtype=dtype).element_size()
+        self._ptr = C.c_void_p()
+        L.call("stater_host_alloc", self.bytes, C.byref(self._ptr))
+        np_dtype = {torch.float32: np.float32, torch.int32: np.int32, torch.float64: np.float64}[dtype]
+        buf = (C.c_char * self.bytes).from_address(self._ptr.value)
+        self.tensor = torch.from_numpy(np.frombuffer(buf, dtype=np_dtype).reshape(shape))
+
+    def close(self) -> None:
+        if self._ptr:
+            self.tensor = None
+            L.call("stater_host_free", self._ptr, self.bytes)
+            self._ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def setup() -> None:
     L.call("stater_setup")
 

@@ -557,12 +557,24 @@ void stater_server::run() {
                 const bool fits = used + j->footprint <= budget || active.empty();
                 if (free_slot < 0 || !fits) break;
                 slots[free_slot].busy = true;
-                // small single-round jobs waiting together share the slot as one group
+                // Small single-round jobs waiting together share a slot as one
+                // group, but only as many as the free slots cannot take one by
+                // one: a run of q such jobs at the head of the queue with f free
+                // slots forms groups of ceil(q / f), so fusion never serialises
+                // jobs that could run side by side.
                 std::vector<std::shared_ptr<Job>> group;
                 if (fusable(*j)) {
+                    int nfree = 0, q = 0;
+                    for (const auto &sl : slots) nfree += sl.busy ? 0 : 1;
+                    nfree += 1;  // the slot just taken
+                    for (const auto &qj : queue) {
+                        if (!fusable(*qj) || q == kFuseMaxJobs * nfree) break;
+                        q++;
+                    }
+                    const int gsize = std::min(kFuseMaxJobs, (q + nfree - 1) / nfree);
                     group.push_back(j);
                     queue.pop_front();
-                    while (!queue.empty() && (int)group.size() < kFuseMaxJobs && fusable(*queue.front()) &&
+                    while (!queue.empty() && (int)group.size() < gsize && fusable(*queue.front()) &&
                            used + group_footprint(group) + queue.front()->footprint <= budget) {
                         group.push_back(queue.front());
                         queue.pop_front();
