@@ -1203,6 +1203,17 @@ bool stream_capturing(cudaStream_t s) {
     return st != cudaStreamCaptureStatusNone;
 }
 
+// The cached height of a shape class, else the default (never tunes, never
+// synchronises).
+int cached_ring_ty(int filter, int km, int nrec, int R, int variant, size_t px) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const TuneKey key{dev, filter, km, nrec, R, variant, size_class(px)};
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    auto it = g_tuned.find(key);
+    return it != g_tuned.end() ? it->second : ring_ty(R, nrec);
+}
+
 // launch(ty) enqueues the filter with tile height ty on s and returns its error.
 template <typename LaunchFn>
 int pick_ring_ty(int filter, int km, int nrec, int R, int variant, size_t px, cudaStream_t s, LaunchFn launch) {
@@ -1840,7 +1851,12 @@ stater_status plan_enqueue_denoise(BatchPlan &B, int n, cudaStream_t s, bool tun
         for (auto &c : B.classes) {
             if (c.filter != pass) continue;
             int ty = c.ty;
-            if (tune || !ty) {
+            if (!tune && !ty) {
+                const int variant = 64 + (c.filter == 0 ? (c.levc ? 1 : 0) + (c.zp ? 2 : 0) : (c.jb ? 1 : 0)) +
+                                    (c.feats ? 4 : 0);
+                ty = c.ty = cached_ring_ty(c.filter, c.km, c.nrec, c.R, variant, c.pixels);
+            }
+            if (tune) {
                 const int variant = 64 + (c.filter == 0 ? (c.levc ? 1 : 0) + (c.zp ? 2 : 0) : (c.jb ? 1 : 0)) +
                                     (c.feats ? 4 : 0);
                 ty = pick_ring_ty(c.filter, c.km, c.nrec, c.R, variant, c.pixels, s,
@@ -1943,7 +1959,8 @@ stater_status batch_denoise_once(const stater_batch_job *jobs, int n, cudaStream
         return cuda_status(e, "batch_denoise_once: table upload");
     }
     plan_bind(B2, dev);
-    st = plan_enqueue_denoise(B2, n, s, !stream_capturing(s));
+    // no tuning here: it would synchronise the serving engine's scheduler thread
+    st = plan_enqueue_denoise(B2, n, s, false);
     cudaFreeAsync(dev, s);
     return st;
 }
