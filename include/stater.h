@@ -410,6 +410,11 @@ typedef struct {
     int32_t *targetspp;
 } stater_target_spp_args;
 stater_status stater_calc_target_spp_ex(const stater_target_spp_args *a, stater_stream stream);
+/* stat_denoiser::calcTargetSPP<float3> over the reference's pitched GpuMat layout
+ * (stater_pitched_layout; estimator.cpp:502-511): n and targetspp are int32
+ * images of n_step, m2, varD and mean RGB images of rgb_step. */
+stater_status stater_calc_target_spp_pitched(const stater_target_spp_args *a, const stater_pitched_layout *layout,
+                                             stater_stream stream);
 
 /* No counterpart in the reference. The same computation as
  * stater_calc_target_spp for callers that cannot allocate device memory (pool

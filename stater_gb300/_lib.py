@@ -137,6 +137,7 @@ def load() -> C.CDLL:
         "stater_denoise_film": (st, [C.POINTER(DenoiseFilmArgs), VP]),
         "stater_denoise_vars_pitched": (st, [C.POINTER(DenoiseVarsArgs), C.POINTER(PitchedLayout), VP]),
         "stater_denoise_film_pitched": (st, [C.POINTER(DenoiseFilmArgs), C.POINTER(PitchedLayout), VP]),
+        "stater_calc_target_spp_pitched": (st, [C.POINTER(TargetSppArgs), C.POINTER(PitchedLayout), VP]),
         "stater_tcrit_lut_intervals": (C.c_int32, []),
         "stater_tcrit2_table": (st, [C.c_double, VP]),
         "stater_t_quantile": (C.c_double, [C.c_double, C.c_double]),

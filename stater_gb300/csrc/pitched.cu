@@ -253,3 +253,38 @@ extern "C" stater_status stater_denoise_film_pitched(const stater_denoise_film_a
     if (st != STATER_OK) return st;
     return launch_copies(plan.out, base, W, H, false, s, "stater_denoise_film_pitched scatter");
 }
+
+extern "C" stater_status stater_calc_target_spp_pitched(const stater_target_spp_args *a,
+                                                        const stater_pitched_layout *L, stater_stream stream) {
+    clear_error();
+    if (!a) return set_error(STATER_ERR_INVALID, "stater_calc_target_spp_pitched: null args");
+    if (a->precision != STATER_F32 && a->precision != STATER_F64)
+        return set_error(STATER_ERR_INVALID, "stater_calc_target_spp_pitched: bad precision");
+    if (a->width <= 0 || a->height <= 0)
+        return set_error(STATER_ERR_INVALID, "stater_calc_target_spp_pitched: bad geometry");
+    const int elem = a->precision == STATER_F64 ? 8 : 4;
+    stater_status st = check_layout(L, a->width, elem, "stater_calc_target_spp_pitched");
+    if (st != STATER_OK) return st;
+    const int W = a->width, H = a->height;
+    const bool sample = a->as_source == STATER_AS_SAMPLE;
+    Plan plan((size_t)W * H);
+    stater_target_spp_args b = *a;
+    b.n = (const int32_t *)plan.add(plan.in, a->n, 1, 4, L->n_step);
+    b.m2 = sample ? plan.add(plan.in, a->m2, 3, elem, L->rgb_step) : nullptr;
+    b.varD = sample ? nullptr : plan.add(plan.in, a->varD, 3, elem, L->rgb_step);
+    b.mean = plan.add(plan.in, a->mean, 3, elem, L->rgb_step);
+    b.targetspp = (int32_t *)plan.add(plan.out, a->targetspp, 1, 4, L->n_step);
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned char *base = (unsigned char *)scratch(22, plan.bytes, s);
+    if (!base) return set_error(STATER_ERR_NOMEM, "stater_calc_target_spp_pitched: scratch allocation failed");
+    b.n = (const int32_t *)resolve((void *)b.n, base);
+    b.m2 = resolve((void *)b.m2, base);
+    b.varD = resolve((void *)b.varD, base);
+    b.mean = resolve((void *)b.mean, base);
+    b.targetspp = (int32_t *)resolve((void *)b.targetspp, base);
+    st = launch_copies(plan.in, base, W, H, true, s, "stater_calc_target_spp_pitched gather");
+    if (st != STATER_OK) return st;
+    st = stater_calc_target_spp_ex(&b, stream);
+    if (st != STATER_OK) return st;
+    return launch_copies(plan.out, base, W, H, false, s, "stater_calc_target_spp_pitched scatter");
+}

@@ -170,3 +170,34 @@ def test_pitched_rejects_short_steps(st):
     layout.rgb_step, layout.scalar_step, layout.n_step = 3 * 64 * 4 - 4, 64 * 4, 64 * 4
     assert L_.load().stater_denoise_vars_pitched(C.byref(va), C.byref(layout), None) == 1
     assert b"rgb_step" in L_.load().stater_last_error()
+
+
+@pytest.mark.parametrize("as_source", [0, 1])
+def test_pitched_target_spp_equals_planar(st, as_source):
+    L_ = st._lib
+    W, H = 91, 53
+    rng = np.random.default_rng(5)
+    n = torch.from_numpy(rng.integers(1, 200, size=(H, W)).astype(np.int32)).cuda()
+    m2 = torch.from_numpy(rng.random((3, H, W)).astype(np.float32) * 3).cuda()
+    varD = torch.from_numpy(rng.random((3, H, W)).astype(np.float32)).cuda()
+    mean = torch.from_numpy(rng.random((3, H, W)).astype(np.float32) + 0.05).cuda()
+    ref = torch.zeros(H, W, dtype=torch.int32, device="cuda")
+
+    def args(nn, mm2, vd, mu, out):
+        a = L_.TargetSppArgs()
+        a.width, a.height, a.spp, a.precision = W, H, 64, st.F32
+        a.n, a.m2, a.varD, a.mean = nn.data_ptr(), mm2.data_ptr(), vd.data_ptr(), mu.data_ptr()
+        a.eps, a.tmin, a.tmax, a.as_source, a.targetspp = 1e-4, 16, 1024, as_source, out.data_ptr()
+        return a
+
+    a = args(n, m2, varD, mean, ref)
+    assert L_.load().stater_calc_target_spp_ex(C.byref(a), None) == 0
+    P = Pitched(H, W, torch.float32, pad=7)
+    n_p = P.one(n, dtype=torch.int32, pitch=P.n_p)
+    out_p = P.one(None, dtype=torch.int32, pitch=P.n_p)
+    a = args(n_p, P.rgb(m2), P.rgb(varD), P.rgb(mean), out_p)
+    layout = P.layout(st)
+    assert L_.load().stater_calc_target_spp_pitched(C.byref(a), C.byref(layout), None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(out_p[:, :W], ref)
+    assert bool((out_p[:, W:] == -12345).all())
