@@ -118,6 +118,20 @@ def test_accumulate_fast_f32_vs_f64_oracle(st):
     assert moment_err(host(b.stats).astype(np.float64), so, n, 3, resolution=1e-3) <= F32_TOL
 
 
+def test_accumulate_fast_1024spp(st):
+    """The FP32 form's uncompensated online update at the largest sample count of
+    the serving trace: moments within 1e-4 of their scale after 1024 samples."""
+    W, H, G = 32, 24, 7
+    s = synth_samples(W, H, 1024, G=G, seed=15)
+    b = st.StatBuffers(W, H, BASE_TR, G, 3, st.F32)
+    b.accumulate(dev(s), mode=st.ACC_FAST)
+    n, so, go = oracle.new_state(5, G, H, W)
+    oracle.accumulate(s, BASE_TR, 3, n, so, go)
+    assert np.array_equal(host(b.n), n)
+    assert moment_err(host(b.stats).astype(np.float64), so, n, 3, resolution=1e-3) <= F32_TOL
+    assert np.max(np.abs(host(b.gmean).astype(np.float64) - go)) <= 1e-5
+
+
 @pytest.mark.parametrize("W,H", [(96, 40), (37, 23)])
 def test_accumulate_fast_with_counts(st, W, H):
     """FP32 form with uneven per-pixel counts over two rounds (the TMA-fed path
@@ -353,3 +367,25 @@ def test_fp32_film_filter_forms_agree(st, W, H, tr, mm, R, mt_mode):
     b.denoise_film(radius=R, gbuffers=specs, mt_mode=mt_mode, accept_bits=bits)
     torch.cuda.synchronize()
     assert torch.equal(ring, b.filmD)
+
+
+@pytest.mark.parametrize("W,H", [(64, 40), (100, 36)])
+def test_lev_tma_equals_plain_kernel(st, W, H):
+    """The TMA-fed LEV accumulation (two pixels per lane in packed FP32) and the
+    plain one-thread-per-pixel kernel (taken when the sample planes are not
+    16-byte aligned) keep the same state bit for bit, with uneven per-pixel
+    counts over two calls."""
+    G = 7
+    s = st.generate_samples(W, H, 37, n_features=G, seed=19, lev_r2=0.6)
+    cnt = torch.from_numpy(np.random.default_rng(3).integers(0, 38, size=(H, W)).astype(np.int32)).cuda()
+    # the same planes one float off 16-byte alignment: the plain kernel
+    buf = torch.empty(s.numel() + 1, dtype=torch.float32, device="cuda")
+    mis = buf[1:].view(s.shape)
+    mis.copy_(s)
+    a = st.LevState(W, H, G, st.F32)
+    b = st.LevState(W, H, G, st.F32)
+    for _ in range(2):
+        a.accumulate(s, count=cnt)
+        b.accumulate(mis, count=cnt)
+    torch.cuda.synchronize()
+    assert torch.equal(a.state, b.state)
