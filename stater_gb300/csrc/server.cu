@@ -41,45 +41,109 @@ __global__ void widen_kernel(size_t n, const float *in, double *out) {
     if (i < n) out[i] = (double)in[i];
 }
 
-// Adaptive rounds visit the pixels sorted by their target (descending), so
-// that the samples still due at any point belong to a prefix of the order and
-// each step covers only that prefix (a 32-pixel group no longer runs to the
-// largest target among its neighbours). Counting sort over targets 0..kTmax.
-constexpr int kBins = 1025;  // targets 0..kTmax
+// Adaptive rounds visit the pixels grouped by the number of sample steps their
+// target still needs (descending), so that the samples still due at any point
+// belong to a prefix of the order and each step covers only that prefix (a
+// 32-pixel group no longer runs to the largest target among its neighbours).
+// Within a group the pixels keep their image order (a stable counting sort), so
+// the columns of a warp are mostly neighbouring pixels and the statistics
+// planes are read and written in long runs.
+constexpr int kBins = 1025;  // targets 0..kTmax (bounds the step count and the act table)
 
-__global__ void target_hist_kernel(size_t HW, const int32_t *target, int32_t *hist) {
-    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= HW) return;
-    atomicAdd(&hist[min(max(target[p], 0), kBins - 1)], 1);
+int sort_bins(int chunk) { return (kTmax + chunk - 1) / chunk + 1; }
+
+__device__ __forceinline__ int steps_of(int t, int chunk, int nbins) {
+    return min((t + chunk - 1) / chunk, nbins - 1);
 }
 
-// One thread: cursor[t] = number of pixels with a target above t (the first
-// position of bin t in the descending order); act[c] = pixels whose target
-// exceeds c * chunk (the active prefix of step c), c = 0..nsteps; *tmax.
-__global__ void target_scan_kernel(const int32_t *hist, int chunk, int32_t *cursor, int32_t *act, int32_t *tmax) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    int32_t above = 0, mx = 0;
-    for (int t = kBins - 1; t >= 0; t--) {
-        cursor[t] = above;
-        if (hist[t] > 0 && mx == 0) mx = t;
-        above += hist[t];
+// Per block of 256 pixels: how many pixels need each number of steps; the
+// largest target of the image (*tmax zeroed before).
+__global__ void __launch_bounds__(256) target_count_kernel(size_t HW, const int32_t *target, int chunk, int nbins,
+                                                           int32_t *block_hist, int32_t *tmax) {
+    extern __shared__ int cnt[];
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) cnt[b] = 0;
+    __syncthreads();
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int t = 0;
+    if (p < HW) {
+        t = min(max(target[p], 0), kTmax);
+        atomicAdd(&cnt[steps_of(t, chunk, nbins)], 1);
     }
-    *tmax = mx;
-    const int nsteps = (kBins - 1 + chunk - 1) / chunk;
-    for (int c = 0; c <= nsteps; c++) {
-        const int d = c * chunk;
-        act[c] = d < kBins ? cursor[d] : 0;
+    for (int o = 16; o > 0; o >>= 1) t = max(t, __shfl_xor_sync(0xffffffffu, t, o));
+    if ((threadIdx.x & 31) == 0 && t > 0) atomicMax(tmax, t);
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) block_hist[(size_t)b * gridDim.x + blockIdx.x] = cnt[b];
+}
+
+// One CTA of 1024 threads, in place: the per-block counts become the first
+// position of every (step count, block) group in the order (step counts
+// descending, blocks ascending); act[c] = the pixels that need more than c
+// steps, c = 0..nbins. Each thread scans a contiguous run of blocks.
+__global__ void __launch_bounds__(1024) target_offsets_kernel(int nblocks, int nbins, int32_t *hist_base,
+                                                              int32_t *act) {
+    __shared__ int warp_sum[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int seg = (nblocks + 1023) / 1024;
+    const int i0 = min(nblocks, (int)threadIdx.x * seg), i1 = min(nblocks, i0 + seg);
+    int running = 0;
+    for (int b = nbins - 1; b >= 0; b--) {
+        int32_t *row = hist_base + (size_t)b * nblocks;
+        int v = 0;
+        for (int i = i0; i < i1; i++) v += row[i];
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int w = warp_sum[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            warp_sum[lane] = w;  // inclusive over warps
+        }
+        __syncthreads();
+        int pos = running + x - v + (warp > 0 ? warp_sum[warp - 1] : 0);
+        for (int i = i0; i < i1; i++) {
+            const int c = row[i];
+            row[i] = pos;
+            pos += c;
+        }
+        running += warp_sum[31];
+        if (threadIdx.x == 0 && b >= 1) act[b - 1] = running;  // pixels with at least b steps
+        __syncthreads();  // warp_sum is rewritten by the next step count
+    }
+    if (threadIdx.x == 0) {
+        act[nbins - 1] = 0;
+        act[nbins] = 0;
     }
 }
 
-__global__ void target_scatter_kernel(size_t HW, const int32_t *target, int32_t *cursor, int32_t *order,
-                                      int32_t *tsorted) {
+// Every pixel's place: its group's first position plus its rank among the
+// group's pixels of the block in image order.
+__global__ void __launch_bounds__(256) target_place_kernel(size_t HW, const int32_t *target, int chunk, int nbins,
+                                                           const int32_t *base, int32_t *order, int32_t *tsorted) {
+    extern __shared__ int wcnt[];  // [8][nbins]
+    for (int i = threadIdx.x; i < 8 * nbins; i += blockDim.x) wcnt[i] = 0;
+    __syncthreads();
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= HW) return;
-    const int t = min(max(target[p], 0), kBins - 1);
-    const int i = atomicAdd(&cursor[t], 1);
-    order[i] = (int32_t)p;
-    tsorted[i] = t;
+    const bool valid = p < HW;
+    const int t = valid ? min(max(target[p], 0), kTmax) : 0;
+    const int key = valid ? steps_of(t, chunk, nbins) : -1;
+    const unsigned same = __match_any_sync(0xffffffffu, key);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lrank = __popc(same & ((1u << lane) - 1u));
+    if (valid && lrank == 0) wcnt[warp * nbins + key] = __popc(same);
+    __syncthreads();
+    if (!valid) return;
+    int r = lrank;
+    for (int w = 0; w < warp; w++) r += wcnt[w * nbins + key];
+    const int pos = base[(size_t)key * gridDim.x + blockIdx.x] + r;
+    order[pos] = (int32_t)p;
+    tsorted[pos] = t;
 }
 
 // Per column of step `done`: samples due (0 for padding beyond the active
@@ -97,7 +161,7 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct Layout {
     size_t HW, T, K, G, chunk;
-    size_t off_n, off_counts, off_target, off_max, off_order, off_tsorted, off_first, off_hist, off_cursor, off_act,
+    size_t off_n, off_counts, off_target, off_max, off_order, off_tsorted, off_first, off_hist, off_act,
         off_stats, off_gmean, off_film, off_rgb, off_rgb64, off_jb, off_out6, off_filmD, off_samples, total;
 };
 
@@ -131,8 +195,8 @@ Layout layout(const stater_job_desc &d, int precision, int chunk_spp) {
     L.off_order = take(4 * (L.HW + 4));
     L.off_tsorted = take(4 * (L.HW + 4));
     L.off_first = take(4 * (L.HW + 4));
-    L.off_hist = take(4 * kBins);
-    L.off_cursor = take(4 * kBins);
+    const size_t nblk = (L.HW + 255) / 256;
+    L.off_hist = take(4 * (size_t)sort_bins((int)L.chunk) * nblk);
     L.off_act = take(4 * (kBins + 2));
     L.off_stats = take(L.K * STATER_NQ * 3 * L.HW * L.T);
     L.off_gmean = take(std::max<size_t>(L.G, 1) * L.HW * L.T);
@@ -408,14 +472,15 @@ bool stater_server::enqueue_after_round(Job &j) {
         // pixels sorted by target; the largest target and each step's active prefix to the host
         int32_t *dmax = (int32_t *)(j.base + L.off_max);
         int32_t *hist = (int32_t *)(j.base + L.off_hist);
-        int32_t *cursor = (int32_t *)(j.base + L.off_cursor);
         int32_t *act = (int32_t *)(j.base + L.off_act);
         const unsigned blocks = (unsigned)((L.HW + 255) / 256);
-        if (cudaMemsetAsync(hist, 0, 4 * kBins, s) != cudaSuccess) return false;
-        target_hist_kernel<<<blocks, 256, 0, s>>>(L.HW, target, hist);
-        target_scan_kernel<<<1, 1, 0, s>>>(hist, (int)L.chunk, cursor, act, dmax);
-        target_scatter_kernel<<<blocks, 256, 0, s>>>(L.HW, target, cursor, (int32_t *)(j.base + L.off_order),
-                                                     (int32_t *)(j.base + L.off_tsorted));
+        const int nbins = sort_bins((int)L.chunk);
+        if (cudaMemsetAsync(dmax, 0, 4, s) != cudaSuccess) return false;
+        target_count_kernel<<<blocks, 256, sizeof(int) * nbins, s>>>(L.HW, target, (int)L.chunk, nbins, hist, dmax);
+        target_offsets_kernel<<<1, 1024, 0, s>>>((int)blocks, nbins, hist, act);
+        target_place_kernel<<<blocks, 256, sizeof(int) * 8 * nbins, s>>>(L.HW, target, (int)L.chunk, nbins, hist,
+                                                                       (int32_t *)(j.base + L.off_order),
+                                                                       (int32_t *)(j.base + L.off_tsorted));
         if (cudaGetLastError() != cudaSuccess) return false;
         if (cudaMemcpyAsync(sl.hmax, dmax, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return false;
         if (cudaMemcpyAsync(sl.hact, act, 4 * (kBins + 2), cudaMemcpyDeviceToHost, s) != cudaSuccess) return false;
