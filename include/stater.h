@@ -141,6 +141,13 @@ int32_t stater_abi_version(void);
  * it has issued always keeps the default limit. Settings are process-wide and
  * apply to launches made after the call. */
 stater_status stater_debug_set_pipeline_waits(uint32_t wait_polls, int32_t stall_producers);
+/* Tuning hook of the TMA-fed FP32 accumulation, no counterpart in the
+ * reference: warp w of each CTA keeps the moments of transform order[w]
+ * (order: a permutation of 0 .. n_transforms-1), for launches with that many
+ * transforms made after the call, in place of the library's own placement.
+ * Results are the same bits for every order. n_transforms = 0 restores the
+ * library's placement. Process-wide. */
+stater_status stater_debug_set_warp_order(const int32_t *order, int32_t n_transforms);
 /* FP32 throughput probe, no counterpart in the reference: launches `blocks`
  * CTAs of 256 threads, each thread running 8 independent chains of 16 * iters
  * FMAs (packed = 1: fma.rn.f32x2, two lanes per instruction), and returns in

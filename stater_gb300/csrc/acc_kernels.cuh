@@ -16,6 +16,10 @@
 // reciprocal shared by all moments of the sample.
 #pragma once
 
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
 #include "common.cuh"
 #include "film_common.cuh"
 #include "packed_f32x2.cuh"
@@ -41,43 +45,131 @@ struct AccParams {
     // transforms' threads carry them (acc_assign_features).
     int8_t featmap[STATER_MAX_TRANSFORMS][STATER_MAX_FEATURES];
     int maxf;  // largest number of channels one transform keeps
+    // TMA-fed kernel: the transform of warp w (a permutation of 0..K-1 that
+    // spreads the costly transforms over the SM's schedulers)
+    int8_t wt[STATER_MAX_TRANSFORMS];
 };
 
-// Relative cost of one sample's update per transform kind (FAST form), used
-// to hand the feature channels to the threads with the cheapest transforms.
-inline float acc_kind_cost(int kind) {
+// Issue cost of one sample's update per transform kind in the FAST form:
+// instructions a warp issues for one sample of its 64 columns (the shared part
+// of 32 -- three loads, the reciprocal of n and the moment updates -- plus the
+// transform's own), and the extras of the film sums and of one feature channel.
+inline int acc_kind_cost(int kind) {
     switch (kind) {
-        case STATER_TK_IDENTITY: return 1.0f;
-        case STATER_TK_SQRT: return 1.15f;
-        case STATER_TK_LOG1P: return 1.5f;
-        case STATER_TK_CBRT: return 1.5f;
-        case STATER_TK_ASINH: return 1.5f;
-        default: return 1.8f;
+        case STATER_TK_IDENTITY: return 32;
+        case STATER_TK_SQRT: return 38;
+        case STATER_TK_CBRT: return 53;
+        case STATER_TK_LOG1P: return 80;
+        case STATER_TK_ASINH: return 101;
+        default: return 200;  // Box-Cox: libm exp and log per value
     }
 }
+constexpr int kAccFilmCost = 27;
+constexpr int kAccFeatureCost = 3;
 
-// Assigns the G feature channels to transforms (greedily to the cheapest
-// current load, at most ceil(G/K) each; transform 0 also carries the film).
-// Returns the largest number of channels one transform keeps.
-inline int acc_assign_features(AccParams &P) {
-    float load[STATER_MAX_TRANSFORMS];
-    int cnt[STATER_MAX_TRANSFORMS];
-    for (int k = 0; k < STATER_MAX_TRANSFORMS; k++) {
-        load[k] = k < P.K ? acc_kind_cost(P.ts.kind[k]) + (k == 0 && P.film.sum ? 0.2f : 0.f) : 1e30f;
-        cnt[k] = 0;
-        for (int j = 0; j < STATER_MAX_FEATURES; j++) P.featmap[k][j] = -1;
+// Where the K transforms' warps and the feature channels go in the TMA-fed
+// kernel. Warp w of a CTA issues on the SM's scheduler w % 4, so two warps
+// whose indices differ by 4 share one; the CTA's time is set by its busiest
+// scheduler. The plan tries every order of the transforms over the warps
+// (K! orders, K <= 8) and, for each, hands the feature channels one by one to
+// the transform on the least busy scheduler (at most ceil(G/K) each, to bound
+// the registers a warp keeps); it keeps the order whose busiest scheduler has
+// the least work. Plans are cached per (transform kinds, G, film).
+struct AccPlan {
+    int8_t wt[STATER_MAX_TRANSFORMS];                            // warp -> transform
+    int8_t featmap[STATER_MAX_TRANSFORMS][STATER_MAX_FEATURES];  // transform -> its feature channels
+    int maxf;
+};
+
+inline int acc_plan_eval(const int *cost, int K, int G, const int8_t *wt, AccPlan *out) {
+    int sched[4] = {0, 0, 0, 0}, cnt[STATER_MAX_TRANSFORMS] = {0};
+    int where[STATER_MAX_TRANSFORMS];
+    for (int w = 0; w < K; w++) {
+        where[wt[w]] = w % 4;
+        sched[w % 4] += cost[wt[w]];
     }
+    const int cap = (G + K - 1) / K;
     int maxc = 0;
-    const int cap = (P.G + P.K - 1) / P.K;  // no transform keeps more than its share
-    for (int g = 0; g < P.G; g++) {
+    if (out)
+        for (int k = 0; k < STATER_MAX_TRANSFORMS; k++)
+            for (int j = 0; j < STATER_MAX_FEATURES; j++) out->featmap[k][j] = -1;
+    for (int g = 0; g < G; g++) {
         int best = -1;
-        for (int k = 0; k < P.K; k++)
-            if (cnt[k] < cap && (best < 0 || load[k] < load[best])) best = k;
-        P.featmap[best][cnt[best]++] = (int8_t)g;
-        load[best] += 0.15f;
+        for (int k = 0; k < K; k++) {
+            if (cnt[k] >= cap) continue;
+            if (best < 0 || sched[where[k]] < sched[where[best]] ||
+                (sched[where[k]] == sched[where[best]] && cost[k] < cost[best]))
+                best = k;
+        }
+        if (out) out->featmap[best][cnt[best]] = (int8_t)g;
+        cnt[best]++;
+        sched[where[best]] += kAccFeatureCost;
         if (cnt[best] > maxc) maxc = cnt[best];
     }
-    return maxc;
+    if (out) out->maxf = maxc;
+    return std::max(std::max(sched[0], sched[1]), std::max(sched[2], sched[3]));
+}
+
+inline AccPlan acc_plan(const int *kinds, int K, int G, bool film) {
+    int cost[STATER_MAX_TRANSFORMS];
+    for (int k = 0; k < K; k++) cost[k] = acc_kind_cost(kinds[k]) + (k == 0 && film ? kAccFilmCost : 0);
+    int8_t order[STATER_MAX_TRANSFORMS], best[STATER_MAX_TRANSFORMS];
+    for (int k = 0; k < K; k++) order[k] = best[k] = (int8_t)k;
+    int best_load = acc_plan_eval(cost, K, G, order, nullptr);
+    while (std::next_permutation(order, order + K)) {
+        const int l = acc_plan_eval(cost, K, G, order, nullptr);
+        if (l < best_load) {
+            best_load = l;
+            std::copy(order, order + K, best);
+        }
+    }
+    AccPlan plan;
+    for (int w = 0; w < STATER_MAX_TRANSFORMS; w++) plan.wt[w] = (int8_t)(w < K ? best[w] : w);
+    acc_plan_eval(cost, K, G, best, &plan);
+    return plan;
+}
+
+// The plan for P's transforms (cached), written into P. Returns the largest
+// number of feature channels one transform keeps.
+inline int acc_assign_features(AccParams &P) {
+    struct Entry {
+        int kinds[STATER_MAX_TRANSFORMS];
+        int K, G;
+        bool film;
+        AccPlan plan;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    const bool film = P.film.sum != nullptr;
+    AccPlan plan;
+    bool found = false;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        for (const Entry &e : cache)
+            if (e.K == P.K && e.G == P.G && e.film == film &&
+                std::equal(e.kinds, e.kinds + P.K, P.ts.kind)) {
+                plan = e.plan;
+                found = true;
+                break;
+            }
+    }
+    if (!found) {
+        plan = acc_plan(P.ts.kind, P.K, P.G, film);
+        std::lock_guard<std::mutex> lock(mu);
+        if (cache.size() < 64) {
+            Entry e;
+            std::copy(P.ts.kind, P.ts.kind + P.K, e.kinds);
+            e.K = P.K;
+            e.G = P.G;
+            e.film = film;
+            e.plan = plan;
+            cache.push_back(e);
+        }
+    }
+    std::copy(plan.wt, plan.wt + STATER_MAX_TRANSFORMS, P.wt);
+    for (int k = 0; k < STATER_MAX_TRANSFORMS; k++)
+        std::copy(plan.featmap[k], plan.featmap[k] + STATER_MAX_FEATURES, P.featmap[k]);
+    return plan.maxf;
 }
 
 // Compact FP32 forms used by the FAST mode, written once over the value type V
@@ -87,15 +179,21 @@ inline int acc_assign_features(AccParams &P) {
 // takes a product as an operand (such pairs are written as FMAs): the code
 // generator may fuse a packed multiply into a following packed add, never a
 // scalar one with explicit rounding, so the sequence leaves it nothing to
-// fuse. Accurate to a few 1e-7 relative, checked against the FP64 oracle:
+// fuse. Accurate to about 1e-6 relative (a few 1e-7 for log1p and asinh),
+// checked against the FP64 oracle:
 //   log1p: 2 atanh(t), t = x/(2+x), by its Taylor series t + t^3/3 + t^5/5
 //          for x < 1/4 (t < 1/9; truncation below 4e-7 relative), else
 //          log2(1+x) ln 2 with the hardware log2;
 //   asinh: for |x| < 1/4 its Taylor series x - x^3/6 + 3x^5/40 - 5x^7/112
 //          (truncation below 5e-7 relative), else log2(|x| + sqrt(x^2 + 1)) ln 2
-//          (2|x| above 1e18, where x^2 would overflow), odd;
-//   cbrt:  2^(log2|x| / 3) refined by one Newton step, odd;
-//   sqrt:  x * rsqrt(x).
+//          (2|x| where x^2 overflows), odd;
+//   cbrt:  2^(log2|x| / 3) with the hardware log2 and exp2, odd (0 at 0,
+//          infinite at infinity: the hardware's log2(0) = -inf, exp2(-inf) = 0);
+//   sqrt:  the hardware square root (0 at 0, NaN below 0).
+// The hardware log2/exp2/sqrt approximations are the special-function unit's,
+// whose issue rate is an eighth of the FMA pipe's: each costs as much as
+// several arithmetic instructions, so each form uses as few as its accuracy
+// allows.
 // Divisions are a multiplication by the hardware reciprocal.
 __device__ __forceinline__ float fast_log2(float x) {
     float y;
@@ -117,6 +215,11 @@ __device__ __forceinline__ float fast_rsqrt(float x) {
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
+__device__ __forceinline__ float fast_sqrt(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
 constexpr float kLn2f = 0.69314718055994531f;
 
@@ -124,9 +227,9 @@ template <typename V>
 __device__ __forceinline__ V log1p_compact(V x) {
     const V t = vmul(x, vmap(vadd(vconst<V>(2.f), x), fast_rcp));
     const V t2 = vmul(t, t);
-    V q = vfma(t2, vconst<V>(1.f / 5.f), vconst<V>(1.f / 3.f));
-    q = vfma(t2, q, vconst<V>(1.f));
-    const V small = vmul(vmul(vconst<V>(2.f), t), q);
+    V q = vfma(t2, vconst<V>(2.f / 5.f), vconst<V>(2.f / 3.f));
+    q = vfma(t2, q, vconst<V>(2.f));
+    const V small = vmul(t, q);  // 2 t (1 + t^2/3 + t^4/5)
     const V large = vmul(vmap(vadd(vconst<V>(1.f), x), fast_log2), vconst<V>(kLn2f));
     return vmap(x, small, large, [](float a, float s, float l) { return a < 0.25f ? s : l; });
 }
@@ -139,26 +242,23 @@ __device__ __forceinline__ V asinh_compact(V x) {
     q = vfma(a2, q, vconst<V>(1.f));
     const V small = vmul(a, q);
     const V w = vfma(a, a, vconst<V>(1.f));
-    const V arg = vmap(a, vfma(w, vmap(w, fast_rsqrt), a),
-                       [](float m, float t) { return m > 1e18f ? __fmul_rn(2.f, m) : t; });
+    // a + sqrt(a^2 + 1) > 2a; where a^2 overflows (a above 1.8e19) the sum is
+    // inf * 0 = NaN, and the maximum (which drops a NaN operand) gives 2a
+    const V arg = vmap(vfma(w, vmap(w, fast_rsqrt), a), vmul(a, vconst<V>(2.f)),
+                       [](float t, float t2) { return fmaxf(t, t2); });
     const V large = vmul(vmap(arg, fast_log2), vconst<V>(kLn2f));
     const V mag = vmap(a, small, large, [](float m, float s, float l) { return m < 0.25f ? s : l; });
     return vmap(mag, x, [](float m, float v) { return copysignf(m, v); });
 }
 template <typename V>
 __device__ __forceinline__ V cbrt_compact(V x) {
-    const V a = vmap(x, [](float v) { return fabsf(v); });
-    const V na = vmap(x, [](float v) { return -fabsf(v); });
-    V y = vmap(vmul(vmap(a, fast_log2), vconst<V>(1.f / 3.f)), fast_exp2);
-    const V y2 = vmul(y, y);
-    // Newton step y - (y^3 - a) / (3 y^2)
-    y = vfma(vfma(y2, y, na), vmap(vmul(vconst<V>(-3.f), y2), fast_rcp), y);
-    return vmap(x, a, y, [](float v, float m, float r) { return m > 0.f ? copysignf(r, v) : v; });
+    const V l = vmap(x, [](float v) { return fast_log2(fabsf(v)); });
+    const V y = vmap(vmul(l, vconst<V>(1.f / 3.f)), fast_exp2);
+    return vmap(y, x, [](float r, float v) { return copysignf(r, v); });
 }
 template <typename V>
 __device__ __forceinline__ V sqrt_compact(V x) {
-    const V r = vmul(x, vmap(x, fast_rsqrt));
-    return vmap(x, r, [](float v, float s) { return v > 0.f ? s : (v == 0.f ? 0.f : __int_as_float(0x7fffffff)); });
+    return vmap(x, fast_sqrt);
 }
 
 // FAST transform of one radiance value (V = float or F2).
@@ -200,15 +300,17 @@ template <typename V, int MAXMOM>
 __device__ __forceinline__ void meng_fast(V x, V rn, V xD, V yD, V &mean, V &m2, V &m3, V &m4, V &cx, V &cy,
                                           V &m1) {
     const V d = vsub(x, mean);
-    const V dN = vmul(d, rn);
     mean = vfma(d, rn, mean);
     if (MAXMOM >= 2) {
         const V e = vfma(d, vmul(rn, vconst<V>(-1.f)), d);  // d - dN
         m2 = vfma(d, e, m2);
         if (MAXMOM >= 3) {
-            const V u = vmul(d, vmul(e, vfma(d, rn, d)));
-            const V m3n = vadd(m3, vfma(vmul(vconst<V>(-3.f), dN), m2, u));
+            // m3 + d (d - dN)(d + dN) - 3 dN m2 = m3 + d ((d - dN)(d + dN) - 3 rn m2):
+            // four operations (the multiples of rn are shared by the channels)
+            const V s = vfma(m2, vmul(rn, vconst<V>(-3.f)), vmul(e, vfma(d, rn, d)));
+            const V m3n = vfma(d, s, m3);
             if (MAXMOM >= 4) {
+                const V dN = vmul(d, rn);
                 const V dN2 = vmul(dN, dN);
                 // d^3 - dN^3 = (d - dN)(d^2 + d dN + dN^2): exactly 0 with e at n = 1
                 const V c3 = vmul(e, vfma(d, d, vfma(d, dN, dN2)));

@@ -2,6 +2,7 @@
 // pairwise moment merge, meanVar. Compiled with -fmad=false: every kernel here
 // rounds each operation separately, like the reference's CPU code and the oracle.
 #include <cmath>
+#include <mutex>
 
 #include "acc_kernels.cuh"
 #include "common.cuh"
@@ -203,9 +204,37 @@ __global__ void mean_var_kernel(size_t HW, const int32_t *n, const float *m2, fl
     var[i] = m2[i] / ((nPF - 1.f) * nPF);
 }
 
+// Warp order set by stater_debug_set_warp_order (n = 0: none).
+std::mutex g_order_mu;
+int g_order_n = 0;
+int8_t g_order[STATER_MAX_TRANSFORMS];
+
+void apply_warp_order(AccParams &P) {
+    std::lock_guard<std::mutex> lock(g_order_mu);
+    if (g_order_n == 0 || g_order_n != P.K) return;
+    // the features stay with their transforms; only the warps change
+    std::copy(g_order, g_order + P.K, P.wt);
+}
+
 }  // namespace stater
 
 using namespace stater;
+
+stater_status stater_debug_set_warp_order(const int32_t *order, int32_t n_transforms) {
+    clear_error();
+    if (n_transforms < 0 || n_transforms > STATER_MAX_TRANSFORMS || (n_transforms > 0 && !order))
+        return set_error(STATER_ERR_INVALID, "stater_debug_set_warp_order: bad arguments");
+    bool seen[STATER_MAX_TRANSFORMS] = {false};
+    for (int w = 0; w < n_transforms; w++) {
+        if (order[w] < 0 || order[w] >= n_transforms || seen[order[w]])
+            return set_error(STATER_ERR_INVALID, "stater_debug_set_warp_order: not a permutation");
+        seen[order[w]] = true;
+    }
+    std::lock_guard<std::mutex> lock(g_order_mu);
+    for (int w = 0; w < n_transforms; w++) g_order[w] = (int8_t)order[w];
+    g_order_n = n_transforms;
+    return STATER_OK;
+}
 
 extern "C" {
 
@@ -260,6 +289,7 @@ stater_status stater_accumulate(const stater_accumulate_args *a, stater_stream s
     P.film.weight = a->film_weight_sum;
     P.film.spill = a->film_spill;
     P.maxf = acc_assign_features(P);
+    apply_warp_order(P);
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e;
     if (a->mode == STATER_ACC_FAST) {

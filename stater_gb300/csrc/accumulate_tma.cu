@@ -6,7 +6,8 @@
 // a few boxes of whole samples) into a kStages-deep ring in shared memory
 // with cp.async.bulk.tensor, completing on per-stage mbarriers. One consumer
 // warp per transform reads the stages (the transform-0 warp also adds the film
-// sums); each lane owns two neighbouring columns and keeps both pixels'
+// sums; which warp keeps which transform comes from the host's plan, which
+// spreads the costly transforms over the SM's four schedulers); each lane owns two neighbouring columns and keeps both pixels'
 // moments in the halves of 64-bit registers, updated by the packed FP32
 // instructions (one issue per pair) with 8-byte shared-memory loads. The
 // update is the same operation sequence as the plain FAST kernel's (the
@@ -39,8 +40,8 @@ using namespace tma;
 #ifndef STATER_TMA_STAGES
 #define STATER_TMA_STAGES 2
 #endif
-#ifndef STATER_TMA_MIN_BLOCKS
-#define STATER_TMA_MIN_BLOCKS 2
+#ifndef STATER_TMA_MAX_REGS
+#define STATER_TMA_MAX_REGS 96
 #endif
 #ifndef STATER_TMA_UNROLL
 #define STATER_TMA_UNROLL 1
@@ -71,7 +72,9 @@ struct PairState {
     Film2 fa;
 };
 
-// film_add of two pixels' samples, element for element the same rounding.
+// film_add of two pixels' samples, element for element the same rounding,
+// except the weight: it gains exactly 1 per sample (integers below 2^24), so
+// the caller adds the number of samples once per stage.
 // The luminance (separately rounded products) is taken element-wise: packed,
 // its multiplies could be fused into the adds.
 __device__ __forceinline__ float film_lum(float r, float g, float b) {
@@ -112,7 +115,6 @@ __device__ __forceinline__ void film_add2(const FilmTarget &F, size_t pa, size_t
     a.s0 = vadd(a.s0, r);
     a.s1 = vadd(a.s1, g);
     a.s2 = vadd(a.s2, b);
-    a.w = vadd(a.w, vconst<F2>(1.f));
     float ua, ub, va, vb;
     f2_unpack(u, ua, ub);
     f2_unpack(v, va, vb);
@@ -128,24 +130,18 @@ __device__ __forceinline__ void film_add2(const FilmTarget &F, size_t pa, size_t
     }
 }
 
-// One sample of one column of the pair (h: 0 the lane's first column, 1 its
-// second), in the scalar form, with n = nn.
-template <int MAXMOM, int MAXF, int KIND>
-__device__ __forceinline__ void sample_one(const AccParams &P, const float *row, int h, uint32_t nn,
+// One sample of one column of the pair (H: 0 the lane's first column, 1 its
+// second), in the scalar form, with n = nn. The column is a template argument:
+// a runtime index into the lane's per-column arrays would place them in local
+// memory.
+template <int MAXMOM, int MAXF, int KIND, int H>
+__device__ __forceinline__ void sample_one(const AccParams &P, const float *row, uint32_t nn,
                                            const int (&foff)[MAXF > 0 ? MAXF : 1], size_t p, float lam, bool film,
                                            PairState<MAXF> &S) {
     constexpr int NL = MAXMOM >= 5 ? 5 : 3;
-    auto get = [h](F2 x) {
-        float lo, hi;
-        f2_unpack(x, lo, hi);
-        return h ? hi : lo;
-    };
-    auto put = [h](F2 &x, float v) {
-        float lo, hi;
-        f2_unpack(x, lo, hi);
-        x = f2_pack(h ? lo : v, h ? v : hi);
-    };
-    row += h;
+    auto get = [](F2 x) { return f2_get<H>(x); };
+    auto put = [](F2 &x, float v) { f2_set<H>(x, v); };
+    row += H;
     float cur[NL];
 #pragma unroll
     for (int q = 0; q < NL; q++) cur[q] = row[q * kPx];
@@ -242,14 +238,17 @@ __device__ __forceinline__ bool tma_consume(const AccParams &P, uint32_t wait_li
                 for (int jf = 0; jf < MAXF; jf++)
                     if (foff[jf] >= 0) S.fm[jf] = vfma(vsub(f2_load(row + foff[jf]), S.fm[jf]), rn, S.fm[jf]);
             }
+            if constexpr (FILM) S.fa.w = vadd(S.fa.w, vconst<F2>((float)jlo));
         }
         // the column with more samples in this stage takes the rest alone
-        if (ja != jb) {
-            const int h = ja > jb ? 0 : 1;
-            const int jn = max(ja, jb);
-            for (int j = jlo; j < jn; j++)
-                sample_one<MAXMOM, MAXF, KIND>(P, stage + (size_t)j * NCH * kPx, h, n0[h] + (uint32_t)(c * kSB + j) + 1u,
-                                               foff, p[h], lam, FILM, S);
+        if (ja > jb) {
+            for (int j = jlo; j < ja; j++)
+                sample_one<MAXMOM, MAXF, KIND, 0>(P, stage + (size_t)j * NCH * kPx, n0[0] + (uint32_t)(c * kSB + j) + 1u,
+                                                  foff, p[0], lam, FILM, S);
+        } else if (jb > ja) {
+            for (int j = jlo; j < jb; j++)
+                sample_one<MAXMOM, MAXF, KIND, 1>(P, stage + (size_t)j * NCH * kPx, n0[1] + (uint32_t)(c * kSB + j) + 1u,
+                                                  foff, p[1], lam, FILM, S);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[sidx]);
@@ -257,14 +256,19 @@ __device__ __forceinline__ bool tma_consume(const AccParams &P, uint32_t wait_li
     return true;
 }
 
-// Resident CTAs the register allocation is sized for: STATER_TMA_MIN_BLOCKS (3
-// CTAs of K = 5 per SM) where the state fits without spills, else 1.
-constexpr int acc_tma_min_blocks(int maxmom, int maxf) {
-    return (maxmom >= 4 || maxf >= 8) ? 1 : STATER_TMA_MIN_BLOCKS;
+// Registers per thread: 96 keeps 3 CTAs of K = 5 (6 warps each, the producer
+// included) resident per SM, as the shared-memory ring does; measured on
+// GB300, a bound of 104 or 112 already leaves only 2 resident and the kernel
+// runs about 14% slower: the few values spilled at 96 cost less than the lost
+// CTA. The larger states (4 or more moments, 8 or more
+// feature channels per transform) get 224, one CTA per SM. The bound is given
+// per thread rather than as resident blocks of the largest CTA (288 threads).
+constexpr int acc_tma_max_regs(int maxmom, int maxf) {
+    return (maxmom >= 4 || maxf >= 8) ? 224 : STATER_TMA_MAX_REGS;
 }
 
 template <int MAXMOM, int MAXF>
-__global__ void __launch_bounds__(32 * STATER_MAX_TRANSFORMS + 32, acc_tma_min_blocks(MAXMOM, MAXF))
+__global__ void __launch_bounds__(32 * STATER_MAX_TRANSFORMS + 32) __maxnreg__(acc_tma_max_regs(MAXMOM, MAXF))
     acc_tma_kernel(const __grid_constant__ CUtensorMap map, TmaAccParams TP) {
     const AccParams &P = TP.P;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -346,8 +350,8 @@ __global__ void __launch_bounds__(32 * STATER_MAX_TRANSFORMS + 32, acc_tma_min_b
         return;
     }
 
-    // consumers: warp = transform, lane = column pair
-    const int k = warp;
+    // consumers: warp = the plan's transform P.wt[warp], lane = column pair
+    const int k = P.wt[warp];
     float *st = (float *)P.stats;
     float *gm = (float *)P.gmean;
     const bool va = cnt[0] > 0, vb = cnt[1] > 0;
@@ -469,10 +473,13 @@ cudaError_t launch_tma_m(const CUtensorMap &map, const TmaAccParams &TP, cudaStr
 }  // namespace
 
 // Returns cudaErrorNotSupported when the sample planes do not meet the TMA
-// rules (row pitch a multiple of 16 bytes, 16-byte aligned base) or the stages
-// do not fit in shared memory: the caller then uses the plain kernel.
+// rules (row pitch a multiple of 16 bytes, 16-byte aligned base), the stages
+// do not fit in shared memory, or the film is asked for with a transform 0
+// other than the identity: the caller then uses the plain kernel.
 cudaError_t launch_acc_tma_f32(const AccParams &P, int max_moment, cudaStream_t s) {
     if ((P.HW % 4) != 0 || ((uintptr_t)P.samples % 16) != 0) return cudaErrorNotSupported;
+    // the film sums ride along with an identity transform 0 only
+    if (P.film.sum && P.ts.kind[0] != STATER_TK_IDENTITY) return cudaErrorNotSupported;
     const size_t smem = (size_t)kStages * kSB * P.NCH * kPx * sizeof(float);
     if (smem > 200 * 1024) return cudaErrorNotSupported;
     // a stage is loaded as kSB / spb boxes of spb whole samples, at most 256 rows each

@@ -113,6 +113,19 @@ def test_pipeline_wait_hook_rejects(lib):
     assert lib.stater_debug_set_pipeline_waits(0, 0) == 0
 
 
+def test_warp_order_hook_rejects(lib):
+    """The warp-order hook takes only permutations of 0 .. n-1 (n <= 8)."""
+    import numpy as np
+    bad = [np.array([0, 1, 1], np.int32), np.array([0, 3, 1], np.int32), np.array([-1, 0, 1], np.int32)]
+    for o in bad:
+        assert lib.stater_debug_set_warp_order(o.ctypes.data, 3) == INVALID
+    assert lib.stater_debug_set_warp_order(None, 2) == INVALID
+    assert lib.stater_debug_set_warp_order(np.zeros(9, np.int32).ctypes.data, 9) == INVALID
+    ok = np.array([2, 0, 1], np.int32)
+    assert lib.stater_debug_set_warp_order(ok.ctypes.data, 3) == 0
+    assert lib.stater_debug_set_warp_order(None, 0) == 0
+
+
 def test_pitched_entry_points_reject_bad_layouts(lib):
     va = L.DenoiseVarsArgs()
     va.n_buffers, va.width, va.height, va.max_moment, va.precision = 1, 64, 8, 3, L.F32
