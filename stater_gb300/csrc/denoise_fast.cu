@@ -311,10 +311,12 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P)
                     for (int c = 0; c < 3; c++) {
                         const float dl = li[q][c] - lj[c];
                         const float t = fmaf(-dl, dl, ZPIX ? zz : __fadd_rn(zi[q][c], zj[c]));
-                        const float m = t >= 0.f ? w : 0.f;
-                        aw[q][c] += m;
-                        av[q][c] = fmaf(m, vj[c], av[q][c]);
-                        if (LEVC) avc[q][c] = fmaf(m, vcj[c], avc[q][c]);
+                        // an accepted neighbour adds its weight (a rejected one adds nothing)
+                        if (t >= 0.f) {
+                            aw[q][c] += w;
+                            av[q][c] = fmaf(w, vj[c], av[q][c]);
+                            if (LEVC) avc[q][c] = fmaf(w, vcj[c], avc[q][c]);
+                        }
                     }
                 }
             }
@@ -793,10 +795,11 @@ __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by
                     for (int c = 0; c < 3; c++) {
                         const float dl = li[k][c] - lj[c];
                         const float t = fmaf(-dl, dl, ZPIX ? zz : __fadd_rn(zi[k][c], zj[c]));
-                        const float m = t >= 0.f ? w : 0.f;
-                        aw[k][c] += m;
-                        av[k][c] = fmaf(m, vj[c], av[k][c]);
-                        if (LEVC) avc[k][c] = fmaf(m, vcj[c], avc[k][c]);
+                        if (t >= 0.f) {  // the same updates as the per-transform kernel
+                            aw[k][c] += w;
+                            av[k][c] = fmaf(w, vj[c], av[k][c]);
+                            if (LEVC) avc[k][c] = fmaf(w, vcj[c], avc[k][c]);
+                        }
                     }
                 }
             }
