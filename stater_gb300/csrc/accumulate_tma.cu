@@ -131,51 +131,45 @@ __device__ __forceinline__ void film_add2(const FilmTarget &F, size_t pa, size_t
 }
 
 // One sample of one column of the pair (H: 0 the lane's first column, 1 its
-// second), in the scalar form, with n = nn. The column is a template argument:
-// a runtime index into the lane's per-column arrays would place them in local
-// memory.
+// second), in the scalar form, with n = nn: the operations of acc_update's
+// FAST form, one channel at a time (fewer values live than unpacking the
+// whole state first). The column is a template argument: a runtime index into
+// the lane's per-column arrays would place them in local memory.
 template <int MAXMOM, int MAXF, int KIND, int H>
 __device__ __forceinline__ void sample_one(const AccParams &P, const float *row, uint32_t nn,
                                            const int (&foff)[MAXF > 0 ? MAXF : 1], size_t p, float lam, bool film,
                                            PairState<MAXF> &S) {
-    constexpr int NL = MAXMOM >= 5 ? 5 : 3;
     auto get = [](F2 x) { return f2_get<H>(x); };
     auto put = [](F2 &x, float v) { f2_set<H>(x, v); };
     row += H;
-    float cur[NL];
-#pragma unroll
-    for (int q = 0; q < NL; q++) cur[q] = row[q * kPx];
     if (film) {
         FilmAcc fa{get(S.fa.s0), get(S.fa.s1), get(S.fa.s2), get(S.fa.w)};
-        film_add(P.film, p, cur[0], cur[1], cur[2], row[3 * kPx], row[4 * kPx], fa);
+        film_add(P.film, p, row[0], row[kPx], row[2 * kPx], row[3 * kPx], row[4 * kPx], fa);
         put(S.fa.s0, fa.s0);
         put(S.fa.s1, fa.s1);
         put(S.fa.s2, fa.s2);
         put(S.fa.w, fa.w);
     }
-    float mean[3], m2[3], m3[3], m4[3], cx[3], cy[3], m1[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        mean[c] = get(S.mean[c]);
-        m2[c] = get(S.m2[c]);
-        m3[c] = get(S.m3[c]);
-        m4[c] = get(S.m4[c]);
-        cx[c] = get(S.cx[c]);
-        cy[c] = get(S.cy[c]);
-        m1[c] = get(S.m1[c]);
+    const float rn = fast_rcp((float)nn);
+    float xD = 0.f, yD = 0.f;
+    if (MAXMOM >= 5) {
+        xD = __fsub_rn(row[3 * kPx], 0.5f);
+        yD = __fsub_rn(row[4 * kPx], 0.5f);
     }
-    float rn;
-    acc_update<float, true, MAXMOM, KIND>(cur, nn, lam, mean, m2, m3, m4, cx, cy, m1, rn);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        put(S.mean[c], mean[c]);
-        if (MAXMOM >= 2) put(S.m2[c], m2[c]);
-        if (MAXMOM >= 3) put(S.m3[c], m3[c]);
-        if (MAXMOM >= 4) put(S.m4[c], m4[c]);
+        float mean = get(S.mean[c]), m2 = get(S.m2[c]), m3 = get(S.m3[c]), m4 = get(S.m4[c]);
+        float cx = get(S.cx[c]), cy = get(S.cy[c]), m1 = get(S.m1[c]);
+        meng_fast<float, MAXMOM>(fast_transform<float, KIND>(lam, row[c * kPx]), rn, xD, yD, mean, m2, m3, m4, cx,
+                                 cy, m1);
+        put(S.mean[c], mean);
+        if (MAXMOM >= 2) put(S.m2[c], m2);
+        if (MAXMOM >= 3) put(S.m3[c], m3);
+        if (MAXMOM >= 4) put(S.m4[c], m4);
         if (MAXMOM >= 5) {
-            put(S.cx[c], cx[c]);
-            put(S.cy[c], cy[c]);
-            put(S.m1[c], m1[c]);
+            put(S.cx[c], cx);
+            put(S.cy[c], cy);
+            put(S.m1[c], m1);
         }
     }
 #pragma unroll
