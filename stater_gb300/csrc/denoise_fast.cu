@@ -739,8 +739,9 @@ __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by
     const size_t HW = (size_t)P.W * P.H;
     const size_t gi = in ? (size_t)y * P.W + x : 0;
 
-    // (the variance filter is bound by shared-memory bandwidth, not by the
-    // latency of these loads: they are stored as they arrive)
+    // (the variance filter is not bound by the latency of these loads: they
+    // are stored as they arrive; fetching the next row into registers during
+    // the window row's arithmetic measured slower, at 128 registers)
     auto value = [&](int rec, int col, int hrow) { return vars_ring_value<LEVC, ZPIX>(P, rec, col, hrow, x0, y0); };
     for (int hrow = 0; hrow < TY; hrow++) ring_load_now(ring, hrow % NS, hrow, hw, nrec, value);
 
@@ -782,6 +783,9 @@ __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by
                     }
                 }
                 const float w = fast_exp2(e);
+                // per-pixel z (ZPIX): the threshold sum z_i + z_j is the same for
+                // every transform (every record carries the same z_j)
+                const float zz = ZPIX ? __fadd_rn(zp, rp[(size_t)kRingFW * hw + dx].w) : 0.f;
 #pragma unroll
                 for (int k = 0; k < KMAX; k++) {
                     if (k >= K) break;
@@ -790,7 +794,6 @@ __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by
                     const float4 T2 = TW == 3 ? tp[2 * hw] : f4(0.f, 0.f, 0.f, 0.f);
                     const float lj[3] = {T0.x, T0.y, T0.z}, vj[3] = {T1.x, T1.y, T1.z}, vcj[3] = {T2.x, T2.y, T2.z};
                     const float zj[3] = {T0.w, T1.w, T2.w};
-                    const float zz = __fadd_rn(zi[k][0], T0.w);
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         const float dl = li[k][c] - lj[c];
