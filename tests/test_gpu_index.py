@@ -85,3 +85,38 @@ def test_generator_index_mode(S):
     for i in (0, 1, 2, 3, 100, W * H - 1):
         c = int(cnt[i])
         assert torch.equal(packed[:c, :, i], d[:c, :, i])
+
+
+def _acc_with_order(S, lib, order, W, H, G, mm, s, cnt):
+    """One FP32 accumulation (TMA-fed: W*H a multiple of 4) with the warp order
+    `order` set for the call (None: the library's plan)."""
+    if order is not None:
+        a = np.array(order, np.int32)
+        assert lib.stater_debug_set_warp_order(a.ctypes.data, len(order)) == 0
+    try:
+        b = S.StatBuffers(W, H, TR, G, mm, S.F32)
+        f = S.Film(W, H, G)
+        b.accumulate(torch.from_numpy(s).cuda(), count=torch.from_numpy(cnt).cuda(), mode=S.ACC_FAST, film=f)
+        torch.cuda.synchronize()
+        return b, f
+    finally:
+        assert lib.stater_debug_set_warp_order(None, 0) == 0
+
+
+@pytest.mark.parametrize("mm,G", [(3, 7), (5, 7), (3, 16)])
+def test_warp_order_gives_the_same_bits(S, mm, G):
+    """The TMA-fed kernel's placement of transforms on warps (the library's
+    plan, or any order set with stater_debug_set_warp_order) changes no bit of
+    the moments, feature means, counts or film sums, with uneven counts. An
+    order for another number of transforms leaves the plan in place."""
+    from stater_gb300 import _lib as L
+    lib = L.load()
+    W, H, N = 64, 40, 30
+    s = synth_samples(W, H, N, G=G, seed=95)
+    cnt = np.random.default_rng(96).integers(0, N + 1, size=(H, W)).astype(np.int32)
+    ref_b, ref_f = _acc_with_order(S, lib, [0, 1, 2, 3, 4], W, H, G, mm, s, cnt)
+    for order in (None, [4, 3, 2, 1, 0], [2, 4, 0, 1, 3], [1, 0]):
+        b, f = _acc_with_order(S, lib, order, W, H, G, mm, s, cnt)
+        assert torch.equal(b.stats, ref_b.stats), order
+        assert torch.equal(b.gmean, ref_b.gmean) and torch.equal(b.n, ref_b.n), order
+        assert torch.equal(f.contrib_sum, ref_f.contrib_sum) and torch.equal(f.weight_sum, ref_f.weight_sum), order
