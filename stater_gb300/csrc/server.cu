@@ -231,6 +231,12 @@ struct Job {
     unsigned char *base = nullptr;
     cudaEvent_t ev = nullptr;
     std::shared_ptr<int> group_left;  // fused group: jobs of the group not finished yet
+    // A pageable result buffer is filled from the slot's pinned staging once the
+    // job's GPU work is done: a device-to-host copy into pageable memory would
+    // run through the driver's synchronous staging (and fault in the caller's
+    // fresh pages) on the scheduler thread, up to 20 ms for a 1080p result.
+    bool out_pinned = true;
+    float *out_stage = nullptr;
     Clock::time_point t_submit, t_done;
     double latency_ms = 0;
 };
@@ -240,6 +246,8 @@ struct Slot {
     int32_t *hmax = nullptr;  // pinned: largest target of the last round
     int32_t *hact = nullptr;  // pinned: active prefix length of each step of the next round
     void *staging = nullptr;  // pinned: job tables of a fused group
+    float *out = nullptr;     // pinned: results bound for pageable buffers (grown while the slot is idle)
+    size_t out_cap = 0;       // floats
     bool busy = false;
 };
 
@@ -499,7 +507,8 @@ bool stater_server::enqueue_after_round(Job &j) {
         if (stater_denoise_film(&f, (stater_stream)s) != STATER_OK) return false;
         if (j.d.out_host) {
             if (L.T == 4) {
-                if (cudaMemcpyAsync(j.d.out_host, f.filmD, 3 * L.HW * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+                void *dst = j.out_stage ? (void *)j.out_stage : j.d.out_host;
+                if (cudaMemcpyAsync(dst, f.filmD, 3 * L.HW * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
                     return false;
             } else {
                 // plain FP64 form: the film is delivered as float32 like the FP32 form
@@ -516,10 +525,43 @@ bool stater_server::fusable(const Job &j) const {
            j.d.n_transforms <= 5 && j.d.n_features <= 7;
 }
 
+// Pinned staging of the slot for the results of `jobs` bound for pageable
+// buffers; the slot is idle, so its staging is free to grow.
+bool stage_results(Slot &sl, const std::vector<Job *> &jobs) {
+    size_t need = 0;
+    for (Job *j : jobs)
+        if (j->d.out_host && !j->out_pinned) need += 3 * j->L.HW;
+    if (need > sl.out_cap) {
+        if (sl.out) cudaFreeHost(sl.out);
+        sl.out = nullptr;
+        sl.out_cap = 0;
+        if (cudaMallocHost((void **)&sl.out, need * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            sl.out = nullptr;
+            return false;
+        }
+        sl.out_cap = need;
+    }
+    size_t o = 0;
+    for (Job *j : jobs) {
+        j->out_stage = nullptr;
+        if (j->d.out_host && !j->out_pinned) {
+            j->out_stage = sl.out + o;
+            o += 3 * j->L.HW;
+        }
+    }
+    return true;
+}
+
 bool stater_server::start_group(std::vector<std::shared_ptr<Job>> &group) {
     const int slot = group[0]->slot;
     Slot &sl = slots[slot];
     cudaStream_t s = sl.stream;
+    {
+        std::vector<Job *> js;
+        for (auto &g : group) js.push_back(g.get());
+        if (!stage_results(sl, js)) return false;
+    }
     std::vector<stater_batch_job> bj(group.size());
     for (size_t i = 0; i < group.size(); i++) {
         Job &j = *group[i];
@@ -548,8 +590,8 @@ bool stater_server::start_group(std::vector<std::shared_ptr<Job>> &group) {
     for (auto &jp : group) {
         Job &j = *jp;
         if (j.d.out_host &&
-            cudaMemcpyAsync(j.d.out_host, j.base + j.L.off_filmD, 3 * j.L.HW * 4, cudaMemcpyDeviceToHost, s) !=
-                cudaSuccess)
+            cudaMemcpyAsync(j.out_stage ? (void *)j.out_stage : j.d.out_host, j.base + j.L.off_filmD, 3 * j.L.HW * 4,
+                            cudaMemcpyDeviceToHost, s) != cudaSuccess)
             return false;
         j.round = 1;
         j.final_enqueued = true;
@@ -560,6 +602,7 @@ bool stater_server::start_group(std::vector<std::shared_ptr<Job>> &group) {
 
 bool stater_server::start(Job &j) {
     Slot &sl = slots[j.slot];
+    if (!stage_results(sl, {&j})) return false;
     if (cudaMallocAsync((void **)&j.base, j.L.total, sl.stream) != cudaSuccess) {
         cudaGetLastError();
         j.base = nullptr;
@@ -685,6 +728,7 @@ void stater_server::run() {
                 continue;
             }
             if (j->final_enqueued) {
+                if (j->out_stage) std::memcpy(j->d.out_host, j->out_stage, 3 * j->L.HW * sizeof(float));
                 finish(*j, true);
                 continue;
             }
@@ -755,6 +799,12 @@ stater_status stater_server_submit(stater_server *srv, const stater_job_desc *jo
         return set_error(STATER_ERR_UNSUPPORTED, "stater_server_submit: host output is float32 (serve in STATER_F32)");
     auto j = std::make_shared<Job>();
     j->d = *job;
+    if (job->out_host) {
+        cudaPointerAttributes pa;
+        const cudaError_t e = cudaPointerGetAttributes(&pa, job->out_host);
+        if (e != cudaSuccess) cudaGetLastError();
+        j->out_pinned = e == cudaSuccess && pa.type == cudaMemoryTypeHost;
+    }
     j->L = layout(*job, srv->cfg.precision, srv->cfg.chunk_spp);
     j->footprint = (double)j->L.total + (double)scratch_bytes(j->L);
     j->t_submit = Clock::now();
@@ -859,6 +909,7 @@ stater_status stater_server_destroy(stater_server *srv) {
         if (sl.hmax) cudaFreeHost(sl.hmax);
         if (sl.hact) cudaFreeHost(sl.hact);
         if (sl.staging) cudaFreeHost(sl.staging);
+        if (sl.out) cudaFreeHost(sl.out);
     }
     delete srv;
     return STATER_OK;

@@ -150,3 +150,32 @@ def test_fused_small_jobs_equal_alone(S):
     assert st["completed"] == len(jobs) and st["failed"] == 0
     for i, (o, a) in enumerate(zip(outs, alone)):
         assert np.array_equal(o, a), i
+
+
+@pytest.mark.parametrize("fuse", [False, True])
+def test_pinned_and_pageable_results_agree(S, fuse):
+    """A result bound for page-locked memory is written by the device copy, one
+    bound for pageable memory from the engine's page-locked staging: the same
+    bits either way, alone and in a fused group, with the engine reused."""
+    from stater_gb300 import serving
+    A = dict(width=128, height=96, spp=32, transforms=BASE_TR, radius=5, seed=31)
+    B = dict(width=96, height=64, spp=16, transforms=BASE_TR, radius=4, seed=32)
+    with serving.Server(max_slots=2, fuse_small_jobs=fuse) as srv:
+        res = {}
+        for kind in ("pageable", "pinned", "pageable"):
+            outs = []
+            for m in (A, B, A):
+                if kind == "pinned":
+                    o = torch.zeros((3, m["height"], m["width"]), dtype=torch.float32, pin_memory=True).numpy()
+                else:
+                    o = _out(m["width"], m["height"])
+                outs.append(o)
+            ids = [srv.submit(serving.job_desc(**m, out=o), keepalive=o) for m, o in zip((A, B, A), outs)]
+            for jid in ids:
+                srv.wait(jid)
+            res.setdefault(kind, []).append(outs)
+    for outs in res["pageable"] + res["pinned"]:
+        assert np.array_equal(outs[0], res["pinned"][0][0])
+        assert np.array_equal(outs[2], res["pinned"][0][0])
+        assert np.array_equal(outs[1], res["pinned"][0][1])
+        assert np.isfinite(outs[1]).all() and outs[1].any()
