@@ -1624,12 +1624,26 @@ __global__ void film_discr_batch(const FastFilm *__restrict__ jobs, const int *_
     film_discr_body(P, (size_t)(blockIdx.x - __ldg(start + j)) * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
+// The CTA's job parameters, copied from the job table into shared memory: the
+// ring bodies read them from there as the single-image kernels read theirs
+// from the parameter space, rather than keeping global-memory copies of them
+// in registers (which spilled).
+template <typename Params>
+__device__ __forceinline__ void load_job_params(const Params *__restrict__ src, Params &dst) {
+    static_assert(sizeof(Params) % 4 == 0, "parameter block of whole words");
+    const int *s = reinterpret_cast<const int *>(src);
+    int *d = reinterpret_cast<int *>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(Params) / 4); i += blockDim.x) d[i] = __ldg(s + i);
+    __syncthreads();
+}
+
 // jobs: the class's jobs only; start[j]: first ring tile of job j
 template <bool LEVC, bool ZPIX, int KMAX, int TY>
 __global__ void __launch_bounds__(kTX2 *TY) vars_ring_batch(const FastVars *__restrict__ jobs,
                                                             const int *__restrict__ start, int njobs) {
+    __shared__ FastVars P;
     const int j = batch_job(start, njobs, blockIdx.x);
-    const FastVars &P = jobs[j];
+    load_job_params(jobs + j, P);
     const int tx = (P.W + kTX2 - 1) / kTX2, local = blockIdx.x - __ldg(start + j);
     vars_ring_body<LEVC, ZPIX, KMAX, TY>(P, local % tx, local / tx);
 }
@@ -1637,8 +1651,9 @@ __global__ void __launch_bounds__(kTX2 *TY) vars_ring_batch(const FastVars *__re
 template <int KMAX, int TY, bool JB>
 __global__ void __launch_bounds__(kTX2 *TY, 16 / TY) film_ring_batch(const FastFilm *__restrict__ jobs,
                                                                     const int *__restrict__ start, int njobs) {
+    __shared__ FastFilm P;
     const int j = batch_job(start, njobs, blockIdx.x);
-    const FastFilm &P = jobs[j];
+    load_job_params(jobs + j, P);
     const int tx = (P.W + kTX2 - 1) / kTX2, local = blockIdx.x - __ldg(start + j);
     film_ring_body<KMAX, TY, JB>(P, local % tx, local / tx);
 }
