@@ -657,12 +657,23 @@ __device__ __forceinline__ void ring_feat_fields(const FeatSet &fs, bool inb, si
 
 // Vars ring fields per transform k: {lnS2 x3, z^2 se2 (ZPIX) | c0}, {s2 x3, 0 | c1},
 // [{s2C x3, 0 | c2}] with c = z^2 se2 per channel when it depends on it.
+// With one z^2 se2 per pixel and no LEVC sums (PACKED) the records are packed
+// instead: the six values of every transform slot k < KMAX (lnS2 x3, s2 x3)
+// back to back, then the pixel's z^2 se2: ceil((6 KMAX + 1) / 4) records, 8
+// for 5 transforms where the per-transform form takes 10 (one shared load in
+// six fewer per neighbour; the filter is bound by its shared loads).
 template <bool LEVC, bool ZPIX>
 struct VarsRing {
+    static constexpr bool PACKED = ZPIX && !LEVC;
     static constexpr int TW = (LEVC || !ZPIX) ? 3 : 2;
 };
 
-template <bool LEVC, bool ZPIX>
+// Ring records of a vars job (KMAX: the ring kernel's transform slots).
+__host__ __device__ constexpr int vars_ring_nrec(int K, int KMAX, bool levc, bool zpix) {
+    return kRingFW + ((zpix && !levc) ? (6 * KMAX + 4) / 4 : K * 3);
+}
+
+template <bool LEVC, bool ZPIX, int KMAX>
 __device__ __forceinline__ float4 vars_ring_value(const FastVars &P, int rec, int col, int hrow, int x0, int y0) {
     constexpr int TW = VarsRing<LEVC, ZPIX>::TW;
     const size_t HW = (size_t)P.W * P.H;
@@ -675,6 +686,22 @@ __device__ __forceinline__ float4 vars_ring_value(const FastVars &P, int rec, in
         const float pen = (inb && __ldg(P.n + g) >= 2) ? 0.f : -INFINITY;
         ring_feat_fields(P.feat, inb, g, pen, a, b);
         v = rec == 0 ? a : b;
+    } else if (VarsRing<LEVC, ZPIX>::PACKED) {
+        if (inb) {
+            float e[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int f = (rec - kRingFW) * 4 + i, k = f / 6, sub = f - 6 * k;
+                float x = 0.f;
+                if (f < 6 * KMAX && k < P.K)
+                    x = sub < 3 ? __ldg(P.lnS2[k] + (size_t)sub * HW + g)
+                                : __ldg(P.s2 + ((size_t)k * 3 + (sub - 3)) * HW + g);
+                else if (f == 6 * KMAX)
+                    x = __fmul_rn(__ldg(P.se2[0] + g), P.z2);
+                e[i] = x;
+            }
+            v = f4(e[0], e[1], e[2], e[3]);
+        }
     } else if (inb) {
         const int kr = rec - kRingFW, k = kr / TW, sub = kr - k * TW;
         const float *src = sub == 0 ? P.lnS2[k] : (sub == 1 ? P.s2 + (size_t)k * 3 * HW : P.s2c + (size_t)k * 3 * HW);
@@ -727,11 +754,14 @@ __device__ __forceinline__ void ring_store(const float4 (&pend)[kRingPer], float
 template <bool LEVC, bool ZPIX, int KMAX, int TY>
 __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by) {
     constexpr int TW = VarsRing<LEVC, ZPIX>::TW;
+    constexpr bool PACKED = VarsRing<LEVC, ZPIX>::PACKED;
+    constexpr int NQ = (6 * KMAX + 4) / 4;  // packed records
+    constexpr int ZREC = (6 * KMAX) / 4, ZCOMP = (6 * KMAX) % 4;
     constexpr int NS = TY + 1;
     extern __shared__ float4 ring[];
     const int R = P.R, hw = kTX2 + 2 * R, hh = TY + 2 * R;
     const int K = P.K, nf = P.feat.nch;
-    const int nrec = kRingFW + K * TW;
+    const int nrec = vars_ring_nrec(K, KMAX, LEVC, ZPIX);
     const int x0 = bx * kTX2, y0 = by * TY;
     const int lx = threadIdx.x % kTX2, tr = threadIdx.x / kTX2;
     const int x = x0 + lx, y = y0 + tr;
@@ -742,7 +772,9 @@ __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by
     // (the variance filter is not bound by the latency of these loads: they
     // are stored as they arrive; fetching the next row into registers during
     // the window row's arithmetic measured slower, at 128 registers)
-    auto value = [&](int rec, int col, int hrow) { return vars_ring_value<LEVC, ZPIX>(P, rec, col, hrow, x0, y0); };
+    auto value = [&](int rec, int col, int hrow) {
+        return vars_ring_value<LEVC, ZPIX, KMAX>(P, rec, col, hrow, x0, y0);
+    };
     for (int hrow = 0; hrow < TY; hrow++) ring_load_now(ring, hrow % NS, hrow, hw, nrec, value);
 
     // centre values, read as the per-transform kernel stages them
@@ -783,17 +815,43 @@ __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by
                     }
                 }
                 const float w = fast_exp2(e);
+                // the packed records of the neighbour (PACKED: lnS2 and s2 of every slot, then z)
+                float q[PACKED ? 4 * NQ : 1];
+                if constexpr (PACKED) {
+                    const float4 *qp = rp + (size_t)kRingFW * hw + dx;
+#pragma unroll
+                    for (int i = 0; i < NQ; i++) {
+                        const float4 Q = qp[(size_t)i * hw];
+                        q[4 * i] = Q.x;
+                        q[4 * i + 1] = Q.y;
+                        q[4 * i + 2] = Q.z;
+                        q[4 * i + 3] = Q.w;
+                    }
+                }
                 // per-pixel z (ZPIX): the threshold sum z_i + z_j is the same for
                 // every transform (every record carries the same z_j)
-                const float zz = ZPIX ? __fadd_rn(zp, rp[(size_t)kRingFW * hw + dx].w) : 0.f;
+                const float zz = !ZPIX ? 0.f
+                                 : PACKED ? __fadd_rn(zp, q[4 * ZREC + ZCOMP])
+                                          : __fadd_rn(zp, rp[(size_t)kRingFW * hw + dx].w);
 #pragma unroll
                 for (int k = 0; k < KMAX; k++) {
                     if (k >= K) break;
-                    const float4 *tp = rp + (size_t)(kRingFW + k * TW) * hw + dx;
-                    const float4 T0 = tp[0], T1 = tp[hw];
-                    const float4 T2 = TW == 3 ? tp[2 * hw] : f4(0.f, 0.f, 0.f, 0.f);
-                    const float lj[3] = {T0.x, T0.y, T0.z}, vj[3] = {T1.x, T1.y, T1.z}, vcj[3] = {T2.x, T2.y, T2.z};
-                    const float zj[3] = {T0.w, T1.w, T2.w};
+                    float lj[3], vj[3], vcj[3] = {0.f, 0.f, 0.f}, zj[3] = {0.f, 0.f, 0.f};
+                    if constexpr (PACKED) {
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            lj[c] = q[6 * k + c];
+                            vj[c] = q[6 * k + 3 + c];
+                        }
+                    } else {
+                        const float4 *tp = rp + (size_t)(kRingFW + k * TW) * hw + dx;
+                        const float4 T0 = tp[0], T1 = tp[hw];
+                        const float4 T2 = TW == 3 ? tp[2 * hw] : f4(0.f, 0.f, 0.f, 0.f);
+                        lj[0] = T0.x; lj[1] = T0.y; lj[2] = T0.z;
+                        vj[0] = T1.x; vj[1] = T1.y; vj[2] = T1.z;
+                        vcj[0] = T2.x; vcj[1] = T2.y; vcj[2] = T2.z;
+                        zj[0] = T0.w; zj[1] = T1.w; zj[2] = T2.w;
+                    }
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         const float dl = li[k][c] - lj[c];
@@ -1337,7 +1395,7 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
     const bool zp = P.max_moment < 4;
     {
         const int km = ring_kmax(P.K);
-        const int nrec = kRingFW + P.K * ((P.levc || !zp) ? 3 : 2);
+        const int nrec = vars_ring_nrec(P.K, km, P.levc != 0, zp);
         if (km > 0 && ring_ty(P.R, nrec) > 0 && P.feat.nch <= kRingMF) {
             auto launch = [&](int ty) {
                 const size_t sm = ring_smem(P.R, nrec, ty);
@@ -1725,7 +1783,7 @@ stater_status plan_build(const stater_batch_job *jobs, int n, float *s2base, Bat
         blocks += (int)((HW + 127) / 128);
         B.kmax = std::max(B.kmax, V.K);
         const bool zp = V.max_moment < 4;
-        const int kmv = ring_kmax(V.K), nrv = kRingFW + V.K * ((V.levc || !zp) ? 3 : 2);
+        const int kmv = ring_kmax(V.K), nrv = vars_ring_nrec(V.K, kmv, V.levc != 0, zp);
         const FastFilm &F = B.film[j];
         const int nrf = kRingFW + 1 + 2 * F.K;
         if (!(kmv > 0 && ring_ty(V.R, nrv) > 0 && V.feat.nch <= kRingMF && ring_ty(F.R, nrf) > 0 &&
