@@ -415,11 +415,12 @@ def run_gpu(args, rank, world, dist):
         roofline_filters[name] = {"kernel": kern, "flops_per_pixel": fpp[name] * (2 * R + 1) ** 2, "ms": ms_,
                                   "achieved": ach, "frac": ach / fp32_peak}
     # the variance filter's shared-memory traffic: per neighbour, the feature
-    # record (2 x 16 B) and two 16-byte records per transform, over the SMs'
-    # 128 B/clock at the sampled SM clock
+    # records (2 x 16 B) and the packed records of the transforms (one z per
+    # pixel, no LEVC sums: ceil((6 K + 1) / 4) x 16 B, 8 for K = 5), over the
+    # SMs' 128 B/clock at the sampled SM clock
     props = torch.cuda.get_device_properties(torch.cuda.current_device())
     sm_mhz = clk.summary().get("sm_mhz") or 2070.0
-    smem_bytes = pairs * (2 + 2 * K) * 16
+    smem_bytes = pairs * (2 + (6 * K + 4) // 4) * 16
     roofline_filters["vars"]["smem_frac"] = smem_bytes / (statistics.median(stage_ms["denoise_vars"]) / 1e3) / (
         props.multi_processor_count * 128 * sm_mhz * 1e6)
 
