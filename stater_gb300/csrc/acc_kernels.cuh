@@ -148,7 +148,8 @@ inline int acc_assign_features(AccParams &P) {
         AccPlan plan;
     };
     static std::mutex mu;
-    static std::vector<Entry> cache;
+    static std::vector<Entry> cache;  // at most 64 sets; beyond, entries are overwritten in turn
+    static size_t next_slot = 0;
     const bool film = P.film.sum != nullptr;
     AccPlan plan;
     bool found = false;
@@ -165,15 +166,16 @@ inline int acc_assign_features(AccParams &P) {
     if (!found) {
         plan = acc_plan(P.ts.kind, P.K, P.G, film);
         std::lock_guard<std::mutex> lock(mu);
-        if (cache.size() < 64) {
-            Entry e;
-            std::copy(P.ts.kind, P.ts.kind + P.K, e.kinds);
-            e.K = P.K;
-            e.G = P.G;
-            e.film = film;
-            e.plan = plan;
+        Entry e;
+        std::copy(P.ts.kind, P.ts.kind + P.K, e.kinds);
+        e.K = P.K;
+        e.G = P.G;
+        e.film = film;
+        e.plan = plan;
+        if (cache.size() < 64)
             cache.push_back(e);
-        }
+        else
+            cache[next_slot++ % cache.size()] = e;
     }
     std::copy(plan.wt, plan.wt + STATER_MAX_TRANSFORMS, P.wt);
     for (int k = 0; k < STATER_MAX_TRANSFORMS; k++)
