@@ -148,6 +148,12 @@ stater_status stater_debug_set_pipeline_waits(uint32_t wait_polls, int32_t stall
  * Results are the same bits for every order. n_transforms = 0 restores the
  * library's placement. Process-wide. */
 stater_status stater_debug_set_warp_order(const int32_t *order, int32_t n_transforms);
+/* Tuning hook of the FP32 variance filter's row ring, no counterpart in the
+ * reference: tile_height 4, 8 or 16 forces that tile height (where its ring
+ * fits in shared memory) for the single-image calls made after this one;
+ * 0 restores the tuner. Results are the same bits at every height.
+ * Process-wide. */
+stater_status stater_debug_set_vars_ring_form(int32_t tile_height);
 /* FP32 throughput probe, no counterpart in the reference: launches `blocks`
  * CTAs of 256 threads, each thread running 8 independent chains of 16 * iters
  * FMAs (packed = 1: fma.rn.f32x2, two lanes per instruction), and returns in

@@ -129,6 +129,7 @@ def load() -> C.CDLL:
         "stater_host_free": (st, [VP, C.c_size_t]),
         "stater_debug_set_pipeline_waits": (st, [C.c_uint32, C.c_int32]),
         "stater_debug_set_warp_order": (st, [VP, C.c_int32]),
+        "stater_debug_set_vars_ring_form": (st, [C.c_int32]),
         "stater_fp32_peak_probe": (st, [C.c_int32, C.c_int32, C.c_int32, VP, C.POINTER(C.c_double), VP]),
         "stater_accumulate": (st, [C.POINTER(AccumulateArgs), VP]),
         "stater_generate_samples": (st, [C.POINTER(GenerateArgs), VP]),

@@ -830,9 +830,11 @@ __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by
                 }
                 // per-pixel z (ZPIX): the threshold sum z_i + z_j is the same for
                 // every transform (every record carries the same z_j)
-                const float zz = !ZPIX ? 0.f
-                                 : PACKED ? __fadd_rn(zp, q[4 * ZREC + ZCOMP])
-                                          : __fadd_rn(zp, rp[(size_t)kRingFW * hw + dx].w);
+                float zz = 0.f;
+                if constexpr (PACKED)
+                    zz = __fadd_rn(zp, q[4 * ZREC + ZCOMP]);
+                else if constexpr (ZPIX)
+                    zz = __fadd_rn(zp, rp[(size_t)kRingFW * hw + dx].w);
 #pragma unroll
                 for (int k = 0; k < KMAX; k++) {
                     if (k >= K) break;
@@ -1223,6 +1225,9 @@ constexpr size_t kRingSmemMax = 113 * 1024;
 int ring_kmax(int K) { return K <= 1 ? 1 : K <= 3 ? 3 : K <= 5 ? 5 : 0; }
 
 size_t ring_smem(int R, int nrec, int TY) { return (size_t)(TY + 1) * nrec * (kTX2 + 2 * R) * sizeof(float4); }
+// stater_debug_set_vars_ring_form: a forced tile height of the variance ring
+// (0: the tuner's)
+std::atomic<int> g_vars_form{0};
 
 int ring_ty(int R, int nrec) {
     if (ring_smem(R, nrec, 8) <= kRingSmemMax) return 8;
@@ -1398,9 +1403,9 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
         const int nrec = vars_ring_nrec(P.K, km, P.levc != 0, zp);
         if (km > 0 && ring_ty(P.R, nrec) > 0 && P.feat.nch <= kRingMF) {
             auto launch = [&](int ty) {
+                cudaError_t e = cudaErrorInvalidValue;
                 const size_t sm = ring_smem(P.R, nrec, ty);
                 dim3 grid((P.W + kTX2 - 1) / kTX2, (P.H + ty - 1) / ty);
-                cudaError_t e = cudaErrorInvalidValue;
 #define STATER_RING_VARS(LV, ZV, KV, TV)                                                   \
     if ((P.levc != 0) == LV && zp == ZV && km == KV && ty == TV) {                          \
         e = set_smem(vars_ring_f32<LV, ZV, KV, TV>, sm);                                    \
@@ -1420,7 +1425,9 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
                 return e == cudaSuccess ? cudaGetLastError() : e;
             };
             const int variant = (P.levc ? 1 : 0) + (zp ? 2 : 0) + (P.feat.nch > 0 ? 4 : 0);
-            const int ty = pick_ring_ty(0, km, nrec, P.R, variant, HW, s, launch);
+            int ty = pick_ring_ty(0, km, nrec, P.R, variant, HW, s, launch);
+            const int forced = g_vars_form.load();
+            if (forced != 0 && ring_fits(P.R, nrec, forced)) ty = forced;
             cudaError_t e = launch(ty);
             if (e != cudaSuccess) return cuda_status(e, "vars_ring_f32");
             return STATER_OK;
@@ -1596,6 +1603,15 @@ extern "C" int32_t stater_tuned_tile_height(int32_t filter, int32_t n_transforms
             kv.first.nrec == (filter == 1 ? kRingFW + 1 + 2 * n_transforms : kv.first.nrec))
             return kv.second;
     return 0;
+}
+
+extern "C" stater_status stater_debug_set_vars_ring_form(int32_t tile_height) {
+    using namespace stater;
+    clear_error();
+    if (!(tile_height == 0 || tile_height == 4 || tile_height == 8 || tile_height == 16))
+        return set_error(STATER_ERR_INVALID, "stater_debug_set_vars_ring_form: tile height not 0, 4, 8 or 16");
+    g_vars_form.store(tile_height);
+    return STATER_OK;
 }
 
 extern "C" stater_status stater_test_order(const stater_transform *transforms, int32_t n_transforms,

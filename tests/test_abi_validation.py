@@ -126,6 +126,14 @@ def test_warp_order_hook_rejects(lib):
     assert lib.stater_debug_set_warp_order(None, 0) == 0
 
 
+def test_vars_ring_form_hook_rejects(lib):
+    """The variance-ring form hook takes tile heights 0, 4, 8 and 16 only."""
+    for th in (5, -8, 32, 1):
+        assert lib.stater_debug_set_vars_ring_form(th) == INVALID, th
+    for th in (8, 16, 4, 0):
+        assert lib.stater_debug_set_vars_ring_form(th) == 0, th
+
+
 def test_pitched_entry_points_reject_bad_layouts(lib):
     va = L.DenoiseVarsArgs()
     va.n_buffers, va.width, va.height, va.max_moment, va.precision = 1, 64, 8, 3, L.F32

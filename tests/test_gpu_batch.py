@@ -132,3 +132,31 @@ def test_batch_rejects_fp64_and_capture_of_first_run(st):
     smp = st.generate_samples(W, H, 4, n_features=7, seed=1)
     with pytest.raises((ValueError, st.StaterError)):
         st.Batch([dict(buffers=b, film=film, samples=smp, radius=4)])
+
+
+@pytest.mark.parametrize("W,H,tr,G,R", [
+    (160, 96, TR, 7, 10),
+    (97, 61, TR[:3], 7, 7),     # partial tiles
+    (64, 37, TR[:1], 7, 4),
+])
+def test_vars_ring_forms_give_the_same_bits(st, W, H, tr, G, R):
+    """The FP32 variance ring gives the same varD and varCD bits at every tile
+    height (4, 8, 16, and the tuner's), with uneven counts (pixels below two
+    samples included) and partial tiles."""
+    lib = st.load()
+    smp = st.generate_samples(W, H, 24, n_features=G, seed=41)
+    cnt = torch.from_numpy(np.random.default_rng(42).integers(0, 25, size=(H, W)).astype(np.int32)).cuda()
+    res = []
+    try:
+        for th in (0, 4, 8, 16):
+            assert lib.stater_debug_set_vars_ring_form(th) == 0
+            b = st.StatBuffers(W, H, tr, G, 3, st.F32)
+            b.accumulate(smp, count=cnt, mode=st.ACC_FAST)
+            b.denoise_vars(radius=R)
+            torch.cuda.synchronize()
+            res.append((b.varD.clone(), b.varCD.clone()))
+    finally:
+        assert lib.stater_debug_set_vars_ring_form(0) == 0
+    for vd, vcd in res[1:]:
+        assert torch.equal(vd, res[0][0]) and torch.equal(vcd, res[0][1])
+    assert torch.isfinite(res[0][0]).any()
