@@ -549,8 +549,8 @@ def run_gpu(args, rank, world, dist):
     # one serving rate (each with its own clock record)
     if not args.no_configs:
         extra["lev"] = measure_lev(S, 1920, 1080, 512, steps=3, warmup=1)
-        extra["adaptive"] = measure_adaptive(S, steps=3, warmup=1, chunk=32)
-        extra["serving"] = measure_serving(S, njobs=args.serve_jobs, rate=200.0, slots=4, chunk=32)
+        extra["adaptive"] = measure_adaptive(S, steps=3, warmup=1, chunk=0)
+        extra["serving"] = measure_serving(S, njobs=args.serve_jobs, rate=200.0, slots=4, chunk=0)
         extra["batch"] = measure_batch(S)
 
     cpu = None
@@ -602,7 +602,7 @@ def serving_trace(njobs, seed=0):
     return jobs
 
 
-def run_serving_trace(S, jobs, rate, slots, precision, with_output=True, seed=1, chunk=32, fuse=False):
+def run_serving_trace(S, jobs, rate, slots, precision, with_output=True, seed=1, chunk=0, fuse=False):
     """Submits `jobs` at Poisson arrival times (rate jobs/s; rate <= 0: all at once)
     and returns the server statistics."""
     import numpy as np
@@ -902,7 +902,9 @@ def main():
     ap.add_argument("--rates", default="10,50,200,500", help="serving: comma-separated arrival rates to sweep")
     ap.add_argument("--jobs", type=int, default=40, help="serving: jobs in the trace")
     ap.add_argument("--slots", type=int, default=4, help="serving: concurrent jobs")
-    ap.add_argument("--chunk", type=int, default=32, help="serving / adaptive: samples generated and accumulated per step")
+    ap.add_argument("--chunk", type=int, default=0,
+                    help="serving / adaptive: samples generated and accumulated per step (0: the engine's automatic "
+                         "choice, 128 for adaptive jobs, 32 for one-round jobs)")
     ap.add_argument("--f64-jobs", type=int, default=6, help="serving: jobs timed in the plain FP64 form")
     ap.add_argument("--width", type=int, default=None, help="smaller image for profiling captures")
     ap.add_argument("--height", type=int, default=None)

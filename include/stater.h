@@ -556,7 +556,9 @@ typedef struct {
     int32_t max_slots;          /* concurrent jobs (streams), 1..64 */
     double hbm_budget_bytes;    /* admission limit; <= 0: 80% of the free memory at creation */
     int32_t precision;          /* STATER_F32 (serving form) or STATER_F64 (plain form) */
-    int32_t chunk_spp;          /* samples generated and accumulated per step (default 32) */
+    int32_t chunk_spp;          /* samples generated and accumulated per step; 0: automatic, 128 for adaptive
+                                 * jobs and 32 for one-round jobs; capped at what a round can take and at
+                                 * 16 GiB of sample planes per job */
     /* 1: small single-round FP32 jobs (up to 512x512 pixels, 5 transforms) that
      * wait together are admitted as one group onto one slot, and their denoise
      * stages run as one launch per stage for the group (stater_batch); each

@@ -81,7 +81,7 @@ class Server:
     """Continuous-batching denoise server on the current CUDA device."""
 
     def __init__(self, max_slots: int = 4, hbm_budget_bytes: float = 0.0, precision: int = L.F32,
-                 chunk_spp: int = 32, fuse_small_jobs: bool = False):
+                 chunk_spp: int = 0, fuse_small_jobs: bool = False):
         self.lib = _bind()
         cfg = ServerConfig(max_slots, hbm_budget_bytes, precision, chunk_spp, int(bool(fuse_small_jobs)))
         h = C.c_void_p()
@@ -127,5 +127,5 @@ class Server:
         self.close()
 
 
-def footprint(desc: JobDesc, precision: int = L.F32, chunk_spp: int = 32) -> float:
+def footprint(desc: JobDesc, precision: int = L.F32, chunk_spp: int = 0) -> float:
     return _bind().stater_job_footprint(C.byref(desc), precision, chunk_spp)

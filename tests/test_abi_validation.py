@@ -99,8 +99,15 @@ def test_job_footprint_grows_with_the_job(lib):
     assert 0 < small < large
     assert fewer_tr < more_tr
     assert f64 > small
-    # 1080p, K=5, 32-spp chunk: about 1 GB of statistics/outputs plus a 3.2 GB sample chunk
+    # 1080p, K=5, one round, the automatic 32-spp step: about 1 GB of
+    # statistics/outputs plus a 3.2 GB sample chunk; 128-spp steps: 12.7 GB
     assert 3e9 < large < 6e9
+    assert 12e9 < serving.footprint(serving.job_desc(1920, 1080, 256), chunk_spp=128) < 16e9
+    # a step holds no more samples than a round takes: 16 spp in one round
+    assert small == serving.footprint(serving.job_desc(256, 256, 16), chunk_spp=16)
+    # adaptive jobs take 128-spp steps automatically
+    adaptive = serving.job_desc(256, 256, 16, rounds=3, round_spp=64)
+    assert serving.footprint(adaptive) == serving.footprint(adaptive, chunk_spp=128) > small
 
 
 def test_pipeline_wait_hook_rejects(lib):
