@@ -56,38 +56,78 @@ class ClockSampler:
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
 
+    # Sampling period: a 10-step timed region of the 1080p job lasts about
+    # 160 ms, so the period is well below that. 200 ms is the fallback where
+    # nvidia-smi refuses the shorter period.
+    PERIODS_MS = (50, 200)
+
     def __init__(self, index=0):
         self.index = index
         self.proc = None
+        self.lines = []  # (time.perf_counter() when read, line)
+        self.period_ms = None
+        self.t_start = self.t_end = None
+
+    def _spawn(self, period_ms):
         self.lines = []
+        self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                      "--format=csv,noheader,nounits", "-lms", str(period_ms)],
+                                     stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        self.thread = threading.Thread(target=self._read, args=(self.proc, self.lines), daemon=True)
+        self.thread.start()
+        self.period_ms = period_ms
 
     def __enter__(self):
+        # The timed region starts once the sampler has printed its first line,
+        # so that it is live for the whole region; samples read before the
+        # region (an idle GPU) are left out of the summary.
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
+            for period in self.PERIODS_MS:
+                self._spawn(period)
+                deadline = time.perf_counter() + 3.0
+                while not self.lines and self.proc.poll() is None and time.perf_counter() < deadline:
+                    time.sleep(0.005)
+                if self.lines or self.proc.poll() is None:
+                    break
         except OSError:
             self.proc = None
+        self.t_start = time.perf_counter()
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
+    @staticmethod
+    def _read(proc, lines):
+        for line in proc.stdout:
+            lines.append((time.perf_counter(), line.strip()))
 
     def __exit__(self, *exc):
+        self.t_end = time.perf_counter()
         if self.proc is not None:
+            # one more sample after the region: the one that covers its last period
+            deadline = self.t_end + 2.0 * self.period_ms / 1e3 + 0.1
+            while (self.proc.poll() is None and time.perf_counter() < deadline
+                   and not any(t > self.t_end for t, _ in self.lines)):
+                time.sleep(0.005)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def _region_lines(self):
+        """Lines read inside the timed region plus the first one after it. If
+        the output came in one block (no time stamps to go by), all lines."""
+        if self.t_start is None or self.t_end is None:
+            return [ln for _, ln in self.lines]
+        inside = [ln for t, ln in self.lines if self.t_start < t <= self.t_end]
+        after = [ln for t, ln in self.lines if t > self.t_end][:1]
+        picked = inside + after
+        return picked if picked else [ln for _, ln in self.lines]
 
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self._region_lines():
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 8:
                 continue
@@ -100,9 +140,9 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(name)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "period_ms": self.period_ms}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "period_ms": self.period_ms}
 
 
 # ---------------------------------------------------------------------------
@@ -386,13 +426,13 @@ def run_gpu(args, rank, world, dist):
     acc_ms = statistics.median(stage_ms["accumulate"])
     hbm_peak, peak_source = hbm_peak_gbs()
     # DRAM bytes per launch from one ncu capture of acc_tma_kernel at 480x272, 64 spp,
-    # K=5, G=7, M1-M3: 433.1 MB read + 30.7 MB written, film sums included. The
-    # per-pixel state (228 B each way) is scaled by pixels, the rest of the reads
-    # (the sample planes) by pixel-samples.
+    # K=5, G=7, M1-M3: 433.16 MB read + 28.01 MB written, film sums included.
+    # The per-pixel state (228 B each way) is scaled by pixels, the rest of the
+    # reads (the sample planes) by pixel-samples.
     cap_px = 480 * 272
     state_rd = cap_px * (K * 3 * w["max_moment"] * 4 + G * 4 + 4 + 4 * 4)
-    samp_rd = 433.055488e6 - state_rd
-    traffic = (samp_rd * (HW * SPP) / (cap_px * 64) + (state_rd + 30.747136e6) * HW / cap_px) / 1e9
+    samp_rd = 433.160448e6 - state_rd
+    traffic = (samp_rd * (HW * SPP) / (cap_px * 64) + (state_rd + 28.007680e6) * HW / cap_px) / 1e9
     roofline = {"kernel": "acc_tma_kernel (stage-1 accumulation)", "bound": "hbm",
                 "achieved": acc_bytes / (acc_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                 "frac": acc_bytes / (acc_ms / 1e3) / 1e9 / hbm_peak, "traffic": traffic,
