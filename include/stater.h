@@ -581,7 +581,8 @@ typedef struct {
     uint64_t seed;
     float *out_host;            /* [3][H][W] float32, written when the job completes (may be NULL); page-locked
                                  * memory is written by the device copy, pageable memory from a page-locked
-                                 * staging buffer of the engine once the job's GPU work is done */
+                                 * staging buffer of the engine once the job's GPU work is done; device memory
+                                 * is refused (STATER_ERR_INVALID) */
 } stater_job_desc;
 
 typedef enum { STATER_JOB_QUEUED = 0, STATER_JOB_RUNNING = 1, STATER_JOB_DONE = 2, STATER_JOB_FAILED = 3 } stater_job_state;

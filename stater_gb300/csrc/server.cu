@@ -809,6 +809,9 @@ stater_status stater_server_submit(stater_server *srv, const stater_job_desc *jo
         cudaPointerAttributes pa;
         const cudaError_t e = cudaPointerGetAttributes(&pa, job->out_host);
         if (e != cudaSuccess) cudaGetLastError();
+        // a result in pageable memory is copied there by the host, from staging
+        if (e == cudaSuccess && pa.type == cudaMemoryTypeDevice)
+            return set_error(STATER_ERR_INVALID, "stater_server_submit: out_host is device memory");
         j->out_pinned = e == cudaSuccess && pa.type == cudaMemoryTypeHost;
     }
     j->L = layout(*job, srv->cfg.precision, srv->cfg.chunk_spp);

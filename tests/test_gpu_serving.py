@@ -124,6 +124,11 @@ def test_submit_rejects_bad_jobs(S):
             srv.submit(serving.job_desc(width=0, height=10, spp=4))
         with pytest.raises(StaterError):  # larger than the whole budget
             srv.submit(serving.job_desc(width=512, height=512, spp=4))
+        dev = torch.zeros((3, 8, 8), dtype=torch.float32, device="cuda")
+        d = serving.job_desc(width=8, height=8, spp=4, radius=2)
+        d.out_host = dev.data_ptr()
+        with pytest.raises(StaterError, match="device memory"):  # the result goes to host memory
+            srv.submit(d)
 
 
 def test_fused_small_jobs_equal_alone(S):
