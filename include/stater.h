@@ -151,8 +151,8 @@ stater_status stater_debug_set_warp_order(const int32_t *order, int32_t n_transf
 /* Tuning hook of the FP32 variance filter's row ring, no counterpart in the
  * reference: tile_height 4, 8 or 16 forces that tile height (where its ring
  * fits in shared memory) for the single-image calls made after this one;
- * 0 restores the tuner. Results are the same bits at every height.
- * Process-wide. */
+ * -1 runs the per-transform kernel in place of the ring; 0 restores the
+ * tuner. Results are the same bits in every form. Process-wide. */
 stater_status stater_debug_set_vars_ring_form(int32_t tile_height);
 /* FP32 throughput probe, no counterpart in the reference: launches `blocks`
  * CTAs of 256 threads, each thread running 8 independent chains of 16 * iters

@@ -305,7 +305,9 @@ __global__ void __launch_bounds__(kTX2 *kThreadRows) vars_filter_f32(FastVars P)
 #pragma unroll
                 for (int q = 0; q < kRows; q++) {
                     if (!use[q]) continue;
-                    const float w = fast_exp2(range_arg2<MF>(fi[q], feat, A, h, nf, __fadd_rn(spq[q], dxs)));
+                    const float e = range_arg2<MF>(fi[q], feat, A, h, nf, __fadd_rn(spq[q], dxs));
+                    if (e < -127.f) continue;  // weight 0: adds nothing; skipped as in the ring kernel
+                    const float w = fast_exp2(e);
                     const float zz = __fadd_rn(zi[q][0], zj[0]);
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
@@ -814,6 +816,12 @@ __device__ __forceinline__ void vars_ring_body(const FastVars &P, int bx, int by
                         e = fmaf(-d, d, e);
                     }
                 }
+                // Below -127 the weight exp2(e) is 0 (2^-127 is subnormal, flushed
+                // to zero), and a neighbour of weight 0 adds nothing (its records
+                // are finite: the statistics of a pixel with n < 2 are zeros), so
+                // its records are not loaded; a warp whose lanes all have such a
+                // neighbour skips them. The test on e does not wait for exp2.
+                if (e < -127.f) continue;
                 const float w = fast_exp2(e);
                 // the packed records of the neighbour (PACKED: lnS2 and s2 of every slot, then z)
                 float q[PACKED ? 4 * NQ : 1];
@@ -1226,7 +1234,7 @@ int ring_kmax(int K) { return K <= 1 ? 1 : K <= 3 ? 3 : K <= 5 ? 5 : 0; }
 
 size_t ring_smem(int R, int nrec, int TY) { return (size_t)(TY + 1) * nrec * (kTX2 + 2 * R) * sizeof(float4); }
 // stater_debug_set_vars_ring_form: a forced tile height of the variance ring
-// (0: the tuner's)
+// (0: the tuner's; -1: the per-transform kernel instead of the ring)
 std::atomic<int> g_vars_form{0};
 
 int ring_ty(int R, int nrec) {
@@ -1401,7 +1409,7 @@ stater_status denoise_vars_f32(const stater_denoise_vars_args *a, cudaStream_t s
     {
         const int km = ring_kmax(P.K);
         const int nrec = vars_ring_nrec(P.K, km, P.levc != 0, zp);
-        if (km > 0 && ring_ty(P.R, nrec) > 0 && P.feat.nch <= kRingMF) {
+        if (km > 0 && ring_ty(P.R, nrec) > 0 && P.feat.nch <= kRingMF && g_vars_form.load() >= 0) {
             auto launch = [&](int ty) {
                 cudaError_t e = cudaErrorInvalidValue;
                 const size_t sm = ring_smem(P.R, nrec, ty);
@@ -1608,8 +1616,8 @@ extern "C" int32_t stater_tuned_tile_height(int32_t filter, int32_t n_transforms
 extern "C" stater_status stater_debug_set_vars_ring_form(int32_t tile_height) {
     using namespace stater;
     clear_error();
-    if (!(tile_height == 0 || tile_height == 4 || tile_height == 8 || tile_height == 16))
-        return set_error(STATER_ERR_INVALID, "stater_debug_set_vars_ring_form: tile height not 0, 4, 8 or 16");
+    if (!(tile_height == -1 || tile_height == 0 || tile_height == 4 || tile_height == 8 || tile_height == 16))
+        return set_error(STATER_ERR_INVALID, "stater_debug_set_vars_ring_form: tile height not -1, 0, 4, 8 or 16");
     g_vars_form.store(tile_height);
     return STATER_OK;
 }

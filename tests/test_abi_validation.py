@@ -134,10 +134,11 @@ def test_warp_order_hook_rejects(lib):
 
 
 def test_vars_ring_form_hook_rejects(lib):
-    """The variance-ring form hook takes tile heights 0, 4, 8 and 16 only."""
-    for th in (5, -8, 32, 1):
+    """The variance-ring form hook takes tile heights 0, 4, 8 and 16, and -1
+    (the per-transform kernel), only."""
+    for th in (5, -8, -2, 32, 1):
         assert lib.stater_debug_set_vars_ring_form(th) == INVALID, th
-    for th in (8, 16, 4, 0):
+    for th in (8, 16, 4, -1, 0):
         assert lib.stater_debug_set_vars_ring_form(th) == 0, th
 
 

@@ -141,14 +141,16 @@ def test_batch_rejects_fp64_and_capture_of_first_run(st):
 ])
 def test_vars_ring_forms_give_the_same_bits(st, W, H, tr, G, R):
     """The FP32 variance ring gives the same varD and varCD bits at every tile
-    height (4, 8, 16, and the tuner's), with uneven counts (pixels below two
-    samples included) and partial tiles."""
+    height (4, 8, 16, and the tuner's) as the per-transform kernel, with
+    uneven counts (pixels below two samples included), partial tiles, and
+    neighbours of range weight 0 (other feature regions), whose records both
+    forms skip."""
     lib = st.load()
     smp = st.generate_samples(W, H, 24, n_features=G, seed=41)
     cnt = torch.from_numpy(np.random.default_rng(42).integers(0, 25, size=(H, W)).astype(np.int32)).cuda()
     res = []
     try:
-        for th in (0, 4, 8, 16):
+        for th in (-1, 0, 4, 8, 16):
             assert lib.stater_debug_set_vars_ring_form(th) == 0
             b = st.StatBuffers(W, H, tr, G, 3, st.F32)
             b.accumulate(smp, count=cnt, mode=st.ACC_FAST)
