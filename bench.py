@@ -294,6 +294,48 @@ def filter_flops_per_pair(K, G):
     return {"vars": weight + K * 3 * 7, "film": weight + K * 3 * 7 + 8}
 
 
+def vars_records_loaded(gmean, n, gbuffers, R, filter_sd):
+    """Shares of the variance filter's (pixel, neighbour) positions whose
+    transform records the ring kernel loads: a lane skips them where the range
+    exponent is below -127 (weight 0), a quarter-warp (8 neighbouring pixels of
+    a row, one phase of a 16-byte shared load) where all its lanes do, a warp (32)
+    where all 32 do. Computed in FP32 with torch from the feature means, with
+    the kernel's formula (near the threshold its rounding may differ). Returns
+    {"lanes", "quarter_warps", "warps"}."""
+    import math
+
+    import torch
+    G, H, W = gmean.shape
+    chans, muls = [], []
+    for first, count, sigma in gbuffers:
+        for c in range(count):
+            chans.append(first + c)
+            muls.append(math.sqrt(0.5 / (sigma * sigma) * 1.4426950408889634))
+    f = gmean[chans].float() * torch.tensor(muls, device=gmean.device).view(-1, 1, 1)
+    ok = n >= 2
+    ds2 = -0.5 / (filter_sd * filter_sd) * 1.4426950408889634
+    Wp = (W + 31) // 32 * 32
+    fp = torch.zeros((len(chans), H + 2 * R, Wp + 2 * R), device=gmean.device)
+    fp[:, R:R + H, R:R + W] = f
+    okp = torch.zeros((H + 2 * R, Wp + 2 * R), dtype=torch.bool, device=gmean.device)
+    okp[R:R + H, R:R + W] = ok
+    centre = torch.zeros((H, Wp), dtype=torch.bool, device=gmean.device)
+    centre[:, :W] = ok
+    fc = fp[:, R:R + H, R:R + Wp]
+    groups = (("lanes", 1), ("quarter_warps", 8), ("warps", 32))
+    counts = {key: 0 for key, _ in groups}
+    # groups with a lane that runs the filter, times the neighbour positions
+    totals = {key: int(centre.view(H, Wp // g, g).any(-1).sum().item()) * (2 * R + 1) ** 2 for key, g in groups}
+    for dy in range(-R, R + 1):
+        for dx in range(-R, R + 1):
+            fj = fp[:, R + dy:R + dy + H, R + dx:R + dx + Wp]
+            e = ds2 * (dy * dy + dx * dx) - ((fc - fj) ** 2).sum(0)
+            need = (e >= -127.0) & okp[R + dy:R + dy + H, R + dx:R + dx + Wp] & centre
+            for key, g in groups:
+                counts[key] += int(need.view(H, Wp // g, g).any(-1).sum().item())
+    return {k: counts[k] / max(totals[k], 1) for k in counts}
+
+
 def max_over_ranks(ms, world, dist, device="cuda"):
     """The largest of the ranks' timings: the job is as slow as its slowest replica."""
     import torch
@@ -455,14 +497,19 @@ def run_gpu(args, rank, world, dist):
         roofline_filters[name] = {"kernel": kern, "flops_per_pixel": fpp[name] * (2 * R + 1) ** 2, "ms": ms_,
                                   "achieved": ach, "frac": ach / fp32_peak}
     # the variance filter's shared-memory traffic: per neighbour, the feature
-    # records (2 x 16 B) and the packed records of the transforms (one z per
-    # pixel, no LEVC sums: ceil((6 K + 1) / 4) x 16 B, 8 for K = 5), over the
-    # SMs' 128 B/clock at the sampled SM clock
+    # records (2 x 16 B) and, where the range weight is not 0, the packed
+    # records of the transforms (one z per pixel, no LEVC sums:
+    # ceil((6 K + 1) / 4) x 16 B, 8 for K = 5), counted per quarter-warp phase,
+    # over the SMs' 128 B/clock at the sampled SM clock. The flop counts above
+    # are those of every neighbour (the records of zero-weight neighbours
+    # included).
     props = torch.cuda.get_device_properties(torch.cuda.current_device())
     sm_mhz = clk.summary().get("sm_mhz") or 2070.0
-    smem_bytes = pairs * (2 + (6 * K + 4) // 4) * 16
+    loaded = vars_records_loaded(b.gmean, b.n, w["gbuffers"], R, w["filter_sd"])
+    smem_bytes = pairs * (2 + loaded["quarter_warps"] * ((6 * K + 4) // 4)) * 16
     roofline_filters["vars"]["smem_frac"] = smem_bytes / (statistics.median(stage_ms["denoise_vars"]) / 1e3) / (
         props.multi_processor_count * 128 * sm_mhz * 1e6)
+    roofline_filters["vars"]["records_loaded"] = loaded
 
     del samples
     torch.cuda.empty_cache()
