@@ -57,7 +57,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
 
     # Sampling period: a 10-step timed region of the 1080p job lasts about
-    # 160 ms, so the period is well below that. 200 ms is the fallback where
+    # 150 ms, so the period is well below that. 200 ms is the fallback where
     # nvidia-smi refuses the shorter period.
     PERIODS_MS = (50, 200)
 
