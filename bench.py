@@ -904,6 +904,54 @@ def measure_serving(S, njobs, rate, slots, chunk, seed=0):
             "clocks": clk.summary()}
 
 
+def measure_vars_scenes(S, steps, warmup):
+    """The variance stage (statistics + ring filter) of the 1080p job on two
+    scenes of the same sizes: features constant over 8x8 regions (the
+    benchmark's scene) and one region over the whole image, where no range
+    weight is 0 and no neighbour's records are skipped. Per tile height (the
+    tuner's, then 4, 8 and 16 forced), CUDA events on the launching stream,
+    median of `steps` after `warmup`; with the share of positions whose
+    records are loaded and a checksum of the varD bits."""
+    import torch
+    w = WORKLOAD
+    W, H, SPP, G = w["width"], w["height"], w["spp"], w["features"]
+    lib = S.load()
+    stream = torch.cuda.current_stream()
+    out = {}
+    for name, region in (("regions_8px", 8), ("one_region", max(W, H))):
+        smp = S.generate_samples(W, H, SPP, n_features=G, seed=1234, region=region)
+        b = S.StatBuffers(W, H, w["transforms"], G, w["max_moment"], S.F32)
+        film = S.Film(W, H, n_features=G)
+        b.accumulate(smp, mode=S.ACC_FAST, film=film)
+        torch.cuda.synchronize()
+        del smp
+        torch.cuda.empty_cache()
+        res = {}
+        try:
+            for th in (0, 4, 8, 16):
+                if lib.stater_debug_set_vars_ring_form(th) != 0:
+                    raise RuntimeError(f"variance ring form {th} refused")
+                ts = []
+                for i in range(warmup + steps):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    b.denoise_vars(radius=w["radius"], filter_sd=w["filter_sd"], var_z=w["var_z"], gbuffers=_specs(S))
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    if i >= warmup:
+                        ts.append(e0.elapsed_time(e1))
+                res["tuned_ms" if th == 0 else f"rows{th}_ms"] = statistics.median(ts)
+        finally:
+            lib.stater_debug_set_vars_ring_form(0)
+        res["records_loaded"] = vars_records_loaded(b.gmean, b.n, w["gbuffers"], w["radius"], w["filter_sd"])
+        res["varD_bits_sum"] = int(b.varD.contiguous().view(torch.int32).to(torch.int64).sum().item())
+        out[name] = res
+        del b, film
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_config(args, rank, world, dist):
     import numpy as np
     import torch
@@ -966,6 +1014,17 @@ def run_config(args, rank, world, dist):
                 "config": {"workload": r["workload"]}, "stage_ms": r["stage_ms"], "roofline": r["roofline"],
                 "median_r2": r["median_r2"], "plain_f64": r["plain_f64"],
                 "speedup_vs_plain_f64": r["speedup_vs_plain_f64"], "clocks": r["clocks"]}
+    elif args.config == "vars_scenes":
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+            scenes = measure_vars_scenes(S, args.steps, args.warmup)
+        w = WORKLOAD
+        line = {"metric": "ms per variance stage (stats + ring filter), 1080p K=5 R=10, benchmark scene",
+                "value": scenes["regions_8px"]["tuned_ms"], "unit": "ms", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic (seeded on-device generation)",
+                "config": {"workload": f"variance stage of the {w['width']}x{w['height']} {w['spp']}spp K=5 job, "
+                                       "features constant over 8x8 regions (the benchmark) or over the whole image"},
+                "scenes": scenes, "clocks": clk.summary()}
     if rank == 0 and line is not None:
         print(json.dumps(line), flush=True)
 
@@ -984,7 +1043,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the compact LEV / adaptive / serving legs")
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the compact serving leg")
-    ap.add_argument("--config", default="denoise", choices=["denoise", "serving", "adaptive", "lev"])
+    ap.add_argument("--config", default="denoise", choices=["denoise", "serving", "adaptive", "lev", "vars_scenes"])
     ap.add_argument("--rate", type=float, default=10.0, help="serving: job arrivals per second")
     ap.add_argument("--rates", default="10,50,200,500", help="serving: comma-separated arrival rates to sweep")
     ap.add_argument("--jobs", type=int, default=40, help="serving: jobs in the trace")
