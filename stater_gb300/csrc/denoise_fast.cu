@@ -663,7 +663,8 @@ __device__ __forceinline__ void ring_feat_fields(const FeatSet &fs, bool inb, si
 // instead: the six values of every transform slot k < KMAX (lnS2 x3, s2 x3)
 // back to back, then the pixel's z^2 se2: ceil((6 KMAX + 1) / 4) records, 8
 // for 5 transforms where the per-transform form takes 10 (one shared load in
-// six fewer per neighbour; the filter is bound by its shared loads).
+// six fewer per neighbour of nonzero weight; where every neighbour's records
+// are loaded, the filter is bound by its shared loads).
 template <bool LEVC, bool ZPIX>
 struct VarsRing {
     static constexpr bool PACKED = ZPIX && !LEVC;
