@@ -257,7 +257,9 @@ stater_status stater_generate_samples(const stater_generate_args *a, stater_stre
  * reference's float build (320 bytes: uint64 n at 0, t0 at 64, t1 at 192, seven
  * float3 each), for every tile in order, pixels row-major in the tile. bounds:
  * int32 [n_tiles][4] = x0, y0, x1, y1 (exclusive). Writes n and FP32 stats
- * [n_sets][7][3][W*H], n_sets = 2 (transform tile) or 1 (plain tile). Device pointers. */
+ * [n_sets][7][3][W*H]: n_sets = 2 (transform tile) writes all seven quantities of
+ * t0 and t1; n_sets = 1 (plain tile) writes t0's mean, M2, M3 and M4 and leaves
+ * its c2X, c2Y and m1 planes as they are, as MergeTile does. Device pointers. */
 stater_status stater_merge_tiles(int32_t width, int32_t height, int32_t n_tiles,
                                  const int32_t *bounds, const void *records, int32_t n_sets,
                                  int32_t *n, float *stats, stater_stream stream);

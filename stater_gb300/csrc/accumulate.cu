@@ -146,12 +146,17 @@ __global__ void merge_tiles_kernel(int W, int H, const int32_t *__restrict__ bou
         const unsigned char *r = records + (first + (unsigned long long)j) * 320ull;
         const size_t p = (size_t)y * W + x;
         n[p] = (int32_t) * reinterpret_cast<const unsigned long long *>(r);
+        // a plain tile (MergeTile) sets mean, M2, M3 and M4 only; a transform
+        // tile (MergeTransformTile) all seven quantities of both sets
+        const int nq = n_sets == 1 ? STATER_Q_M4 + 1 : kNQ;
         for (int set = 0; set < n_sets; set++) {
             const float *v = reinterpret_cast<const float *>(r + (set == 0 ? 64 : 192));
 #pragma unroll
-            for (int q = 0; q < kNQ; q++)
+            for (int q = 0; q < kNQ; q++) {
+                if (q >= nq) break;
 #pragma unroll
                 for (int c = 0; c < 3; c++) stats[stat_index(set, q, c, HW) + p] = v[q * 3 + c];
+            }
         }
     }
 }

@@ -266,6 +266,27 @@ class Estimator {
         check_cuda(cudaStreamSynchronize(stream), "MergeTransformTiles");
     }
 
+    // Estimator::MergeTiles (estimator.cpp:268-298) for the untransformed set:
+    // records holds the plain tiles' StatTilePixel<Vec3> records (float build,
+    // 320 bytes each) for every tile in order, bounds the int32 [n_tiles][4]
+    // tile rectangles; host memory. Sets n and the set's mean, M2, M3 and M4, as
+    // MergeTile does. FP32 statistics only.
+    void MergeTiles(const void *records, const int32_t *bounds, int n_tiles) {
+        if (cfg.precision != STATER_F32) throw std::invalid_argument("MergeTiles: FP32 statistics only");
+        const size_t rec_bytes = 320 * HW();
+        auto drec = device_alloc(rec_bytes);
+        auto dbounds = device_alloc((size_t)n_tiles * 4 * sizeof(int32_t));
+        check_cuda(cudaMemcpyAsync(dbounds.get(), bounds, (size_t)n_tiles * 4 * sizeof(int32_t),
+                                   cudaMemcpyHostToDevice, stream),
+                   "MergeTiles bounds");
+        check_cuda(cudaMemcpyAsync(drec.get(), records, rec_bytes, cudaMemcpyHostToDevice, stream),
+                   "MergeTiles records");
+        check(stater_merge_tiles(width, height, n_tiles, (const int32_t *)dbounds.get(), drec.get(), 1, n_ptr(),
+                                 (float *)stats_.get(), (stater_stream)stream),
+              "Estimator::MergeTiles");
+        check_cuda(cudaStreamSynchronize(stream), "MergeTiles");
+    }
+
     // Estimator::Upload (estimator.cpp:346-353): host copies changed since the
     // last upload (buffers read from files) and, with denoisefilm, the film.
     void Upload() {

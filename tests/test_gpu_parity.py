@@ -181,6 +181,22 @@ def test_merge_tiles_matches_reference_records(st):
     assert np.array_equal(host(stats), case["stats"])
 
 
+def test_merge_plain_tiles_sets_mean_to_m4(st):
+    """A plain tile (n_sets = 1, Estimator::MergeTile, estimator.cpp:268-279)
+    sets n and t0's mean, M2, M3 and M4, the values a transform tile writes to
+    its set 0, and leaves the c2X, c2Y and m1 planes as they were."""
+    d = np.load(GOLD / "stattile_inputs.npz")
+    W, H = int(d["W"]), int(d["H"])
+    case = np.load(GOLD / "stattile_boxcox_f32_mm5.npz")
+    n = torch.zeros(H, W, dtype=torch.int32, device="cuda")
+    stats = torch.full((1, 7, 3, H, W), 7.25, dtype=torch.float32, device="cuda")
+    st.merge_tiles(W, H, dev(d["bounds"]), dev(case["records"]), 1, n, stats)
+    got = host(stats)
+    assert np.array_equal(host(n), case["n"].astype(np.int32))
+    assert np.array_equal(got[0, :4], case["stats"][0, :4])
+    assert (got[0, 4:] == np.float32(7.25)).all()
+
+
 def test_merge_moments_matches_oracle(st):
     W, H, G = 33, 21, 0
     a = synth_samples(W, H, 30, G=G, seed=8)
